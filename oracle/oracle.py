@@ -42,11 +42,34 @@ _I64 = ctypes.POINTER(ctypes.c_int64)
 _I32 = ctypes.POINTER(ctypes.c_int32)
 
 
+_variant_libs = {}
+
+
 def lib():
     global _lib
     if _lib is None:
         _lib = ctypes.CDLL(_build())
     return _lib
+
+
+class use_variant:
+    """Context manager: run the C oracle from its FMA-contracted build."""
+
+    def __init__(self, variant="fma"):
+        self.variant = variant
+
+    def __enter__(self):
+        global _lib
+        self.saved = lib()
+        if self.variant not in _variant_libs:
+            _variant_libs[self.variant] = ctypes.CDLL(_build(variant=self.variant))
+        _lib = _variant_libs[self.variant]
+        return self
+
+    def __exit__(self, *exc):
+        global _lib
+        _lib = self.saved
+        return False
 
 
 def _p(a):

@@ -9,8 +9,10 @@
  *  - Entry points without a suffix take HOST pointers: they copy inputs to the
  *    device, run the kernels on the library's stream, copy results back and
  *    synchronise.  Entry points ending in _dev take DEVICE pointers and a
- *    cudaStream_t (passed as void*, NULL = the library stream); they enqueue
- *    work and return without synchronising.
+ *    cudaStream_t (passed as void*; NULL = the CUDA default stream); they
+ *    enqueue work and return without synchronising.  The library's device
+ *    workspace is shared per device: serialise _dev calls that use it
+ *    (p3d_pe_heating_vec_dev, p3d_fuv_field_3d_dev with ray_out == NULL).
  *  - Every function returns 0 on success and a negative P3D_E* code on error;
  *    p3d_last_error() gives the message of the last error on this thread.
  *    There is no CPU fallback: without a usable GPU every call returns

@@ -171,10 +171,14 @@ def pe_heating_vec(pe_table, log_psi_min, log_psi_step, n_psi, eg_min, eg_step, 
 
 def chem_steady(n_h, k_pd_base, k_ci, alpha_cp, k_co_total, r_h2_half_nh, r_cr_base,
                 x_c_total, x_hi, x_h2, x_cp, x_c, x_co, x_o, x_e, x_hcop,
-                max_iter=200, rtol=1e-10, dt0=1e8, growth=4.0):
+                max_iter=200, rtol=1e-12, growth=4.0, selfshield=None, co_implicit=False):
     """FP64 backward-Euler/Newton steady state of the reduced network (new
-    method on the equations of rust/src/chemistry.rs:35-49).  In place;
-    returns (n_converged, iterations, status)."""
+    method on the equations of rust/src/chemistry.rs:35-49).  In place.
+
+    selfshield = (kco_cr, u_h2, u_co, ds, b_dop): k_pd_base / k_co_total
+    then hold the unshielded kpd0 / kco0 and the shielding factors are solved
+    implicitly with the cell's own half layer.  Returns (n_converged,
+    iterations, status, fsh (2, n) or None)."""
     ins = [_f64(a) for a in (n_h, k_pd_base, k_ci, alpha_cp, k_co_total, r_h2_half_nh,
                              r_cr_base, x_hcop)]
     st = [x_hi, x_h2, x_cp, x_c, x_co, x_o, x_e]
@@ -183,14 +187,23 @@ def chem_steady(n_h, k_pd_base, k_ci, alpha_cp, k_co_total, r_h2_half_nh, r_cr_b
     status = np.zeros(n, dtype=np.int32)
     f = lib().or_chem_steady
     f.restype = ctypes.c_int64
+    if selfshield is not None:
+        kcr, uh2, uco, ds, b = selfshield
+        ss = [_f64(a) for a in (kcr, uh2, uco, ds)]
+        fsh = np.zeros(2 * n)
+        extra = [*[_p(a) for a in ss], ctypes.c_double(b), ctypes.c_int(int(co_implicit)),
+                 _p(fsh)]
+    else:
+        fsh = None
+        extra = [None, None, None, None, ctypes.c_double(0.0), ctypes.c_int(0), None]
     r = f(ctypes.c_int64(n), *[_p(a) for a in ins[:7]], ctypes.c_double(x_c_total),
           *[_p(a) for a in st], _p(ins[7]), ctypes.c_int64(max_iter), ctypes.c_double(rtol),
-          ctypes.c_double(dt0), ctypes.c_double(growth), iters.ctypes.data_as(_I64),
+          ctypes.c_double(growth), *extra, iters.ctypes.data_as(_I64),
           status.ctypes.data_as(_I32))
-    return r, iters, status
+    return r, iters, status, (fsh.reshape(2, n) if fsh is not None else None)
 
 
-def thermal_root(ctx10, cii, oi63, oi145, ci, n_bisect=10, max_newton=30, tol=1e-12):
+def thermal_root(ctx10, cii, oi63, oi145, ci, n_bisect=10, max_newton=80, tol=1e-12):
     """Bisection (thermal.rs:231-243) + Newton polish to |dT| <= tol T."""
     ctx = [_f64(a) for a in ctx10]
     lp = [_f64(a) for a in (cii, oi63, oi145, ci)]
@@ -488,3 +501,155 @@ def convergence_stats(st, old_T, old_h2, old_co, tol=0.05):
     dCO = float(np.percentile(rC, 99))
     return [dT, float(np.percentile(rT, 99)), dH2, dCO, float(np.max(rT)), float(np.max(rH)),
             int(np.sum(rT > tol)), max(dT, dH2, dCO)]
+
+
+# ---------------------------------------------------------------------------
+# Steady-state driver (the new method, FP64 CPU restatement)
+# ---------------------------------------------------------------------------
+def selected_columns(density, x_H2, x_CO, ray, dirs, cell_size):
+    """N_H2, N_CO along each cell's selected ray (the ray fixed by A_V, which
+    depends on density only), with the reference's cumsum rounding."""
+    NH2 = np.zeros_like(density)
+    NCO = np.zeros_like(density)
+    for r in np.unique(ray):
+        if r < 0:
+            continue
+        m = ray == r
+        _, _, nh2, nco = _ray_columns(density, x_H2, x_CO, dirs[r], cell_size)
+        NH2[m] = nh2[m]
+        NCO[m] = nco[m]
+    return NH2, NCO
+
+
+def ray_ds(dirs, cell_size):
+    """ds = cell / max(|d_dom|, 0.01) per ray (fuv_rt_3d.py:325-331)."""
+    return np.array([cell_size * (1.0 / max(np.max(np.abs(d)), 0.01)) for d in dirs])
+
+
+def steady_constants(st, zeta0):
+    """Per-cell factors that depend on density only (through G0, A_V, N_H),
+    in the reference's operation order (solver_3d.py:550-557, :704-710;
+    themis_tables.py:333-342)."""
+    G0, AV = st["G0"], st["A_V"]
+    c = {}
+    c["kpd0"] = 4.43e-11 * G0 * np.exp(-3.74 * AV)
+    c["kci"] = 2.56e-10 * G0 * np.exp(-3.02 * AV)
+    c["kco0"] = 1.71e-10 * G0 * np.exp(-3.53 * AV)
+    c["zeta"] = cr_ionization_rate(st["N_H"], zeta0)
+    return c
+
+
+def t_update(T_in, G, mem, w_T=0.5):
+    """Per-cell outer update of T from T_in and G = thermal root at T_in.
+
+    r = G - T_in changes sign at a fixed point; each cell keeps the largest
+    T_in with r > 0 (lo) and the smallest with r < 0 (hi).  With a bracket,
+    the next T is the secant step through the last two (T_in, r) pairs, or
+    the geometric midpoint when that step leaves the bracket.  Without one,
+    the step is the damped T_in + (1 - w_T) r, limited to `span`, which starts
+    at the width of the last lost bracket and grows x4 per step, so a cell
+    whose fixed point drifts searches locally instead of jumping.  Cells
+    whose fixed point sits on a discontinuity of G (the thermal root jumps
+    between branches) converge to the jump instead of oscillating.
+    mem = (T_prev, r_prev, lo, hi, span) per cell."""
+    r = G - T_in
+    Tp, rp, lo, hi, span = mem
+    lo_n = np.where(r > 0, np.maximum(lo, T_in), lo)
+    hi_n = np.where(r < 0, np.minimum(hi, T_in), hi)
+    bad = lo_n >= hi_n
+    had = (lo > 0) & np.isfinite(hi)
+    span = np.where(bad & had, np.maximum(2.0 * (hi - lo), 1e-9 * T_in), span)
+    lo = np.where(bad, np.where(r > 0, T_in, 0.0), lo_n)
+    hi = np.where(bad, np.where(r < 0, T_in, np.inf), hi_n)
+    valid = (lo > 0) & np.isfinite(hi)
+    den = r - rp
+    with np.errstate(divide="ignore", invalid="ignore"):
+        ts = T_in - r * (T_in - Tp) / den
+    ok_sec = np.isfinite(ts) & (den != 0) & (Tp > 0)
+    mid = np.sqrt(lo * np.where(valid, hi, 1.0))
+    inside = ok_sec & (ts > lo) & (ts < hi)
+    step = np.clip((1.0 - w_T) * r, -span, span)
+    span = np.where(valid, span, span * 4.0)
+    Tn = np.where(valid, np.where(inside, ts, mid), T_in + step)
+    Tn = np.where(r == 0, T_in, Tn)
+    return Tn, (T_in.copy(), r, lo, hi, span)
+
+
+def steady_run(density, G0_external, cell_size, nside=1, zeta0=2e-16, T_init=100.0,
+               max_outer=500, tol=1e-10, w_chem=0.5, w_T=0.5, chem_rtol=1e-12,
+               therm_tol=1e-12, tables=None, lines=None, verbose=False, callback=None,
+               co_implicit=False):
+    """FP64 CPU restatement of the GPU steady-state driver.
+
+    Outer fixed-point iteration with the per-iteration physics of
+    PDRSolver3D.run() (solver_3d.py:262-376): columns along each cell's
+    selected ray -> shielding / CR / dust -> chemistry -> thermal balance.
+    Chemistry is solved to F(x) = 0 (backward-Euler / Newton) with the
+    cell's own half layer in its H2 and CO shielding columns solved
+    implicitly; abundances are damped by w_chem (convex combination of the
+    old and new conserved states); T follows the per-cell bracketed secant
+    update of t_update() on the thermal root (bisection + safeguarded
+    Newton).  Stops when the largest relative change of T and of every
+    species above 1e-20 (relative to n_H) is below tol.
+    Returns (state, history)."""
+    if tables is None:
+        from prism3d_gb300.tables import DustTables
+        tables = DustTables()
+    if lines is None:
+        from prism3d_gb300.tables import line_params
+        lines = line_params()
+    dirs, _ = healpix_directions(nside)
+    st = init_state(density, G0_external, zeta0, T_init)
+    shp = density.shape
+    n = st["density"]
+    G0, AV, NH, _, _, ray = fuv_field_3d(n, G0_external, cell_size, None, None, nside,
+                                         return_ray=True)
+    st["G0"], st["A_V"], st["N_H"], st["ray"] = G0, AV, NH, ray
+    analytic_ic(st)
+    const = steady_constants(st, zeta0)
+    st["zeta_CR"] = const["zeta"]
+    ds = ray_ds(dirs, cell_size)[ray]
+    species = ("x_HI", "x_H2", "x_Cp", "x_C", "x_CO")
+    hist = []
+    mem = (np.zeros(shp), np.zeros(shp), np.zeros(shp), np.full(shp, np.inf),
+           np.full(shp, np.inf))
+    for it in range(max_outer):
+        old = {k: st[k].copy() for k in ("T_gas",) + species}
+        NH2, NCO = selected_columns(n, st["x_H2"], st["x_CO"], ray, dirs, cell_size)
+        st["N_H2"], st["N_CO"] = NH2, NCO
+        u_h2 = NH2 - n * st["x_H2"] * ds
+        u_co = NCO - 0.5 * n * st["x_CO"] * ds if co_implicit else NCO
+        t_mean = np.mean(st["T_gas"])
+        b_dop = np.sqrt(2.0 * k_boltz * t_mean / m_H2) / 1e5
+        update_dust(st, tables)
+        a_cp = 4.67e-12 * np.power(st["T_gas"] / 300.0, -0.6)
+        xs = [np.ascontiguousarray(st[k], dtype=np.float64).ravel().copy() for k in
+              species + ("x_O", "x_e")]
+        _, iters, status, fsh = chem_steady(
+            n, const["kpd0"], const["kci"], a_cp, const["kco0"], st["R_H2"] * n * 0.5,
+            2.5 * const["zeta"] * 0.1, X_C, *xs, st["x_HCOp"], rtol=chem_rtol,
+            selfshield=(6.0 * const["zeta"], u_h2, u_co, ds, b_dop), co_implicit=co_implicit)
+        for k, a in zip(species + ("x_O", "x_e"), xs):
+            st[k] = a.reshape(shp)
+        if it > 0 and w_chem > 0:
+            for k in species:
+                st[k] = w_chem * old[k] + (1.0 - w_chem) * st[k]
+        f_h2 = fsh[0].reshape(shp)
+        ctx = thermal_ctx(st, f_h2)
+        t, titers, tstatus = thermal_root(ctx, *lines, tol=therm_tol)
+        st["T_gas"], mem = t_update(old["T_gas"], t.reshape(shp), mem, w_T)
+        d = {"T": float(np.max(np.abs(st["T_gas"] - old["T_gas"]) / old["T_gas"]))}
+        for k in species:
+            ref = np.maximum(old[k], 1e-20)
+            d[k] = float(np.max(np.abs(st[k] - old[k]) / ref))
+        dmax = max(d.values())
+        hist.append(dict(d, dmax=dmax, chem_iters=int(np.max(iters)),
+                         chem_fail=int(np.sum(status)), therm_iters=int(np.max(titers)),
+                         therm_fail=int(np.sum(tstatus))))
+        if verbose:
+            print(it, f"dmax={dmax:.3e}", {k: f"{v:.1e}" for k, v in d.items()})
+        if callback:
+            callback(it, st)
+        if dmax < tol and it > 1:
+            break
+    return st, hist

@@ -311,9 +311,10 @@ void or_net_heating(int64_t n, const double *const *ctx10, const double *t,
     }
 }
 
-/* thermal.rs:189-270.  margin_out (optional) receives the smallest
- * |net| / scale seen at a bracket decision, so tests can tell which cells
- * sit on a sign change within rounding. */
+/* thermal.rs:189-270.  min_abs_net (optional) receives the smallest |net|
+ * met at a bisection decision, so tests can tell which cells have a
+ * bisection midpoint within rounding of the root (there another correct
+ * rounding of the same arithmetic may take the other branch). */
 static double thermal_cell(const thermal_ctx_t *c, const double *cii, const double *oi63,
                            const double *oi145, const double *ci, int64_t n_bisect,
                            int64_t n_newton, double *min_abs_net) {
@@ -330,7 +331,6 @@ static double thermal_cell(const thermal_ctx_t *c, const double *cii, const doub
     for (k = 0; k < n_newton; ++k) {
         double f = net_heating(t, c, cii, oi63, oi145, ci);
         double eps, fp, dfdt, dt;
-        if (fabs(f) < mn) mn = fabs(f);
         if (f > 0.0) t_lo = dmax(t_lo, t); else t_hi = dmin(t_hi, t);
         eps = t * 0.01;
         fp = net_heating(t + eps, c, cii, oi63, oi145, ci);
@@ -417,162 +417,246 @@ void or_pe_heating_vec(const double *table, int64_t n_bins, double log_psi_min,
 /* Steady-state method (new; same equations as chemistry.rs:35-49).         */
 /* ------------------------------------------------------------------------ */
 /*
- * Unknowns after H and C conservation: y = (x_H2, x_C+, x_CO) with
- *   x_HI = 1 - 2 x_H2,   x_C = X_C - x_C+ - x_CO,   x_e = x_C+ + x_HCO+.
- * F(y) = (dx_H2/dt, dx_C+/dt, dx_CO/dt) of chemistry.rs:35-49.
- * Pseudo-transient continuation: backward-Euler steps
- *   (I/dt - J) dy = F(y),  dt <- dt * growth
- * until |F_i| <= rtol * (destruction scale)_i and |dy_i| <= rtol * y_i.
- * Returns the number of BE/Newton iterations in iters_out, and status
- * 0 = converged, 1 = not converged within max_iter.
+ * Unknowns y = (x_HI, x_H2, x_C+, x_C, x_CO).  Rows:
+ *   0  dx_H2/dt = R x_HI - (k_pd + R_cr) x_H2            (rate equation)
+ *   1  x_HI + 2 x_H2 - 1 = 0                             (H conservation)
+ *   2  dx_C+/dt = k_ci x_C - a n_H (x_C+ + x_HCO+) x_C+ + k_co x_CO
+ *   3  dx_CO/dt = k_OH(x_H2) x_C - k_co x_CO,  k_OH = 1e-10 n_H x_OH(x_H2)
+ *   4  x_C+ + x_C + x_CO - X_C = 0                       (C conservation)
+ * i.e. the right-hand side of chemistry.rs:35-49 with its two
+ * renormalisations written as constraints.  Pseudo-transient continuation:
+ * backward-Euler steps on rows 0, 2, 3 ((1/dt) dy - J dy = f) with the
+ * constraints imposed exactly, dt growing by `growth` per accepted step and
+ * shrinking on a non-positive iterate, until every |dy_i| <= rtol y_i and
+ * every rate residual <= rtol of its largest production/destruction term.
+ * status 0 = converged, 1 = iteration limit.
  */
-static void chem_rhs_jac(const double *p, double x_c_total, double x_hcop, const double *y,
-                         double *F, double J[3][3], double *scale) {
-    /* p: n_h, k_pd_base, k_ci, alpha_cp, k_co_total, r_h2_half_nh, r_cr_base */
-    double n_h = p[0], kpd = p[1], kci = p[2], acp = p[3], kco = p[4], rh2 = p[5], rcr = p[6];
-    double h = y[0], cp = y[1], co = y[2];
-    double x_hi = 1.0 - 2.0 * h;
-    double c = x_c_total - cp - co;
-    double xe = cp + x_hcop;
-    double s = 10.0 * h;
-    double x_oh = 1e-9 + 9e-8 * dclamp(s, 0.0, 1.0);
-    double doh = (s > 0.0 && s < 1.0) ? 9e-7 : 0.0;
-    double koh = 1e-10 * x_oh * n_h;
-    double dkoh = 1e-10 * doh * n_h;
-    double an = acp * n_h;
-    F[0] = rh2 * x_hi - kpd * h - rcr * h;
-    F[1] = kci * c - an * xe * cp + kco * co;
-    F[2] = koh * c - kco * co;
-    J[0][0] = -2.0 * rh2 - kpd - rcr; J[0][1] = 0.0; J[0][2] = 0.0;
-    J[1][0] = 0.0;
-    J[1][1] = -kci - an * (xe + cp);
-    J[1][2] = -kci + kco;
-    J[2][0] = dkoh * c;
-    J[2][1] = -koh;
-    J[2][2] = -koh - kco;
-    if (scale) {
-        scale[0] = (2.0 * rh2 + kpd + rcr) * dmax(h, 1e-30) + rh2 * dmax(x_hi, 0.0);
-        scale[1] = kci * dmax(c, 0.0) + an * xe * dmax(cp, 0.0) + kco * dmax(co, 0.0);
-        scale[2] = koh * dmax(c, 0.0) + kco * dmax(co, 0.0);
+typedef struct {
+    double n_h, kpd, kci, acp, kco, rh2, rcr, xc, hcop;
+    /* implicit self-shielding (ss != 0): k_pd = kpd0 f_H2(N_H2),
+     * k_co = kco0 f_CO(N_CO, N_H2) + kco_cr with N_H2 = u_h2 + ds n_H x_H2,
+     * N_CO = u_co + 0.5 ds n_H x_CO (the cell's own half layer) */
+    int ss;
+    double kpd0, kco0, kco_cr, u_h2, u_co, ds, ds_co, b_dop;
+} chem_par_t;
+
+/* f_shield_H2 (shielding.py:17-59) and d f / d N. */
+static double fsh_h2(double n, double b, double *dfdn) {
+    double x = n / 5.0e14;
+    double q = 1.0 + x / b;
+    double sq = sqrt(1.0 + x);
+    double e = exp(-8.5e-4 * sq);
+    double f = 0.965 / (q * q) + 0.035 / sq * e;
+    if (dfdn) {
+        double d = -2.0 * 0.965 / (q * q * q) / b +
+                   0.035 * e * (-0.5 / ((1.0 + x) * sq) - 0.5 * 8.5e-4 / (1.0 + x));
+        *dfdn = (f > 0.0 && f < 1.0) ? d / 5.0e14 : 0.0;
     }
+    return dclamp(f, 0.0, 1.0);
 }
 
-static int solve3(double A[3][3], double *b) {
-    /* Gaussian elimination with partial pivoting, in place. */
-    int r, k, piv;
-    for (k = 0; k < 3; ++k) {
+/* f_shield_CO, Visser-style fit (shielding.py:136-171), with d f / d N_CO and
+ * d f / d N_H2. */
+static double fsh_co(double nco_in, double nh2_in, double *d_co, double *d_h2) {
+    double nco = dmax(nco_in, 1.0), nh2 = dmax(nh2_in, 1.0);
+    double A = 6.428e-8 * pow(nco, 0.53);
+    double B = 3.0e-12 * pow(nh2, 0.495);
+    double Cc = 1e-5 * pow(nco, 0.6);
+    double P4 = pow(nh2, 0.48);
+    double E = exp(-8e-12 * P4);
+    double f = exp(-A) * exp(-B) * (1.0 / (1.0 + Cc * E));
+    int live = (f > 1e-10 && f < 1.0);
+    if (d_co) *d_co = (live && nco_in > 1.0) ?
+        f * (-0.53 * A / nco - 0.6 * Cc * E / (nco * (1.0 + Cc * E))) : 0.0;
+    if (d_h2) *d_h2 = (live && nh2_in > 1.0) ?
+        f * (-0.495 * B / nh2 + Cc * E * 8e-12 * 0.48 * P4 / (nh2 * (1.0 + Cc * E))) : 0.0;
+    return dclamp(f, 1e-10, 1.0);
+}
+
+static void chem5_eval(const chem_par_t *p, const double *y, double *f, double J[5][5],
+                       double *scale, double *fsh_out) {
+    double x_hi = y[0], h = y[1], cp = y[2], c = y[3], co = y[4];
+    double s = 10.0 * h;
+    double x_oh = 1e-9 + 9e-8 * dclamp(s, 0.0, 1.0);
+    double dxoh = (s > 0.0 && s < 1.0) ? 9e-7 : 0.0;
+    double koh = 1e-10 * x_oh * p->n_h;
+    double an = p->acp * p->n_h;
+    double xe = cp + p->hcop;
+    double kpd = p->kpd, kco = p->kco, dkpd_h = 0.0, dkco_h = 0.0, dkco_co = 0.0;
+    int r, k;
+    if (p->ss) {
+        double nh2 = p->u_h2 + p->ds * p->n_h * h;
+        double nco = p->u_co + 0.5 * p->ds_co * p->n_h * co;
+        double d1, dc, dh;
+        double f1 = fsh_h2(nh2, p->b_dop, &d1);
+        double f2 = fsh_co(nco, nh2, &dc, &dh);
+        kpd = p->kpd0 * f1;
+        kco = p->kco0 * f2 + p->kco_cr;
+        dkpd_h = p->kpd0 * d1 * p->ds * p->n_h;
+        dkco_h = p->kco0 * dh * p->ds * p->n_h;
+        dkco_co = p->kco0 * dc * 0.5 * p->ds_co * p->n_h;
+        if (fsh_out) { fsh_out[0] = f1; fsh_out[1] = f2; }
+    }
+    for (r = 0; r < 5; ++r) for (k = 0; k < 5; ++k) J[r][k] = 0.0;
+    f[0] = p->rh2 * x_hi - (kpd + p->rcr) * h;
+    f[1] = x_hi + 2.0 * h - 1.0;
+    f[2] = p->kci * c - an * xe * cp + kco * co;
+    f[3] = koh * c - kco * co;
+    f[4] = cp + c + co - p->xc;
+    J[0][0] = p->rh2; J[0][1] = -(kpd + p->rcr) - h * dkpd_h;
+    J[1][0] = 1.0; J[1][1] = 2.0;
+    J[2][1] = co * dkco_h;
+    J[2][2] = -an * (xe + cp); J[2][3] = p->kci; J[2][4] = kco + co * dkco_co;
+    J[3][1] = 1e-10 * dxoh * p->n_h * c - co * dkco_h;
+    J[3][3] = koh; J[3][4] = -kco - co * dkco_co;
+    J[4][2] = 1.0; J[4][3] = 1.0; J[4][4] = 1.0;
+    scale[0] = p->rh2 * x_hi + (kpd + p->rcr) * h;
+    scale[1] = 1.0;
+    scale[2] = p->kci * c + an * xe * cp + kco * co;
+    scale[3] = koh * c + kco * co;
+    scale[4] = p->xc;
+}
+
+/* Gaussian elimination with partial pivoting on a row-equilibrated copy. */
+static int solve5(double A[5][5], double *b) {
+    int r, k, c;
+    for (r = 0; r < 5; ++r) {
+        double m = 0.0;
+        for (c = 0; c < 5; ++c) if (fabs(A[r][c]) > m) m = fabs(A[r][c]);
+        if (!(m > 0.0)) return 1;
+        for (c = 0; c < 5; ++c) A[r][c] /= m;
+        b[r] /= m;
+    }
+    for (k = 0; k < 5; ++k) {
+        int piv = k;
         double best = fabs(A[k][k]);
-        piv = k;
-        for (r = k + 1; r < 3; ++r) if (fabs(A[r][k]) > best) { best = fabs(A[r][k]); piv = r; }
-        if (best == 0.0) return 1;
+        for (r = k + 1; r < 5; ++r) if (fabs(A[r][k]) > best) { best = fabs(A[r][k]); piv = r; }
+        if (!(best > 0.0)) return 1;
         if (piv != k) {
-            int cc; double tb;
-            for (cc = 0; cc < 3; ++cc) { double tt = A[k][cc]; A[k][cc] = A[piv][cc]; A[piv][cc] = tt; }
+            double tb;
+            for (c = 0; c < 5; ++c) { double t = A[k][c]; A[k][c] = A[piv][c]; A[piv][c] = t; }
             tb = b[k]; b[k] = b[piv]; b[piv] = tb;
         }
-        for (r = k + 1; r < 3; ++r) {
+        for (r = k + 1; r < 5; ++r) {
             double m = A[r][k] / A[k][k];
-            int cc;
-            for (cc = k; cc < 3; ++cc) A[r][cc] -= m * A[k][cc];
+            if (m == 0.0) continue;
+            for (c = k; c < 5; ++c) A[r][c] -= m * A[k][c];
             b[r] -= m * b[k];
         }
     }
-    for (k = 2; k >= 0; --k) {
+    for (k = 4; k >= 0; --k) {
         double s = b[k];
-        int cc;
-        for (cc = k + 1; cc < 3; ++cc) s -= A[k][cc] * b[cc];
+        for (c = k + 1; c < 5; ++c) s -= A[k][c] * b[c];
         b[k] = s / A[k][k];
     }
     return 0;
 }
 
-static int chem_steady_cell(const double *p, double x_c_total, double x_hcop, double *y,
-                            int64_t max_iter, double rtol, double dt0, double growth,
-                            int64_t *iters_out) {
-    double dt = dt0;
+static const int kOdeRow[5] = {1, -1, 2, 4, -1}; /* row -> species it advances */
+
+/* Pseudo-transient continuation: the first step is pure Newton (1/dt = 0);
+ * a step that would make a species non-positive is rejected and retried
+ * with dt = 10 / (fastest rate), which then grows x`growth` per accepted
+ * step.  Converged when every |dy_i| <= rtol max(y_i, 1e-20) and every rate
+ * residual <= rtol of its production + destruction. */
+static int chem_steady_cell(const chem_par_t *p, double *y, int64_t max_iter, double rtol,
+                            double growth, int64_t *iters_out, double *fsh_out) {
+    double inv_dt = 0.0;
     int64_t it;
     int status = 1;
     for (it = 0; it < max_iter; ++it) {
-        double F[3], J[3][3], A[3][3], dy[3], sc[3];
-        double ynew[3];
-        int k, ok = 1, conv;
-        chem_rhs_jac(p, x_c_total, x_hcop, y, F, J, sc);
-        for (k = 0; k < 3; ++k) {
-            int cc;
-            for (cc = 0; cc < 3; ++cc) A[k][cc] = -J[k][cc];
-            A[k][k] += 1.0 / dt;
-            dy[k] = F[k];
+        double f[5], J[5][5], A[5][5], d[5], sc[5], yn[5];
+        int r, c, ok = 1, conv = 1;
+        chem5_eval(p, y, f, J, sc, fsh_out);
+        for (r = 0; r < 5; ++r) {
+            if (kOdeRow[r] >= 0) {
+                for (c = 0; c < 5; ++c) A[r][c] = -J[r][c];
+                A[r][kOdeRow[r]] += inv_dt;
+                d[r] = f[r];
+            } else {
+                for (c = 0; c < 5; ++c) A[r][c] = J[r][c];
+                d[r] = -f[r];
+            }
         }
-        if (solve3(A, dy)) { dt *= 0.1; continue; }
-        /* positivity: H2 in [0, 0.5], C species >= 0 with C+ + CO <= X_C */
-        ynew[0] = y[0] + dy[0];
-        ynew[1] = y[1] + dy[1];
-        ynew[2] = y[2] + dy[2];
-        if (!(ynew[0] > 0.0) || !(ynew[0] < 0.5) || !(ynew[1] > 0.0) || !(ynew[2] > 0.0) ||
-            !(ynew[1] + ynew[2] < x_c_total)) {
-            ok = 0;
+        if (solve5(A, d)) ok = 0;
+        for (r = 0; ok && r < 5; ++r) {
+            yn[r] = y[r] + d[r];
+            if (!(yn[r] > 0.0)) ok = 0;
         }
-        if (!ok) { dt *= 0.25; continue; }
-        conv = 1;
-        for (k = 0; k < 3; ++k) {
-            if (fabs(dy[k]) > rtol * fabs(ynew[k])) conv = 0;
-            if (fabs(F[k]) > rtol * sc[k] + 1e-300) conv = 0;
+        if (!ok) {
+            double lam = 0.0;
+            for (r = 0; r < 5; ++r) if (kOdeRow[r] >= 0) lam = dmax(lam, fabs(J[r][kOdeRow[r]]));
+            inv_dt = (inv_dt == 0.0) ? lam / 10.0 + 1e-30 : inv_dt * 4.0;
+            continue;
         }
-        y[0] = ynew[0]; y[1] = ynew[1]; y[2] = ynew[2];
+        for (r = 0; r < 5; ++r) {
+            if (fabs(d[r]) > rtol * dmax(yn[r], 1e-20)) conv = 0;
+            if (kOdeRow[r] >= 0 && fabs(f[r]) > rtol * sc[r]) conv = 0;
+        }
+        for (r = 0; r < 5; ++r) y[r] = yn[r];
         if (conv) { status = 0; ++it; break; }
-        dt *= growth;
+        inv_dt /= growth;
     }
     if (iters_out) *iters_out = it;
+    if (fsh_out && p->ss) { double f[5], J[5][5], sc[5]; chem5_eval(p, y, f, J, sc, fsh_out); }
     return status;
 }
 
-/* State in/out in the reference's 7-array layout (x_hi..x_e), as the Euler
- * entry point; the abundances are first projected on H and C conservation. */
+/* State in/out in the reference's 7-array layout (x_hi..x_e).  k_pd_base and
+ * k_co_total are used as given when u_h2 == NULL; otherwise k_pd_base holds
+ * kpd0 = 4.43e-11 G0 exp(-3.74 A_V), k_co_total holds kco0 =
+ * 1.71e-10 G0 exp(-3.53 A_V), kco_cr = 6 zeta, and the shielding factors are
+ * evaluated inside the solve from the upstream columns u_h2, u_co, the
+ * selected ray's ds and the Doppler parameter b_dop; with co_implicit == 0,
+ * u_co is the whole N_CO (the cell's own CO layer lagged one outer
+ * iteration).  fsh (2 x n, optional) receives the final (f_H2, f_CO). */
 int64_t or_chem_steady(int64_t n, const double *n_h, const double *k_pd_base, const double *k_ci,
                        const double *alpha_cp, const double *k_co_total,
                        const double *r_h2_half_nh, const double *r_cr_base, double x_c_total,
                        double *x_hi, double *x_h2, double *x_cp, double *x_c, double *x_co,
                        double *x_o, double *x_e, const double *x_hcop, int64_t max_iter,
-                       double rtol, double dt0, double growth, int64_t *iters,
-                       int32_t *status) {
+                       double rtol, double growth, const double *kco_cr, const double *u_h2,
+                       const double *u_co, const double *ds, double b_dop, int co_implicit,
+                       double *fsh, int64_t *iters, int32_t *status) {
     int64_t i, nconv = 0;
 #pragma omp parallel for schedule(dynamic, 1024) reduction(+ : nconv)
     for (i = 0; i < n; ++i) {
-        double p[7] = {n_h[i], k_pd_base[i], k_ci[i], alpha_cp[i], k_co_total[i],
-                       r_h2_half_nh[i], r_cr_base[i]};
-        double y[3];
-        double h = x_h2[i], cp = x_cp[i], co = x_co[i], c = x_c[i];
-        double csum = cp + c + co;
-        int st;
+        chem_par_t p;
+        double y[5] = {x_hi[i], x_h2[i], x_cp[i], x_c[i], x_co[i]};
+        double fo[2] = {0.0, 0.0};
+        int st, k;
         int64_t itc = 0;
-        /* H: x_HI = 1 - 2 x_H2 with x_H2 in (0, 0.5) */
-        h = dclamp(h, 1e-30, 0.5 * (1.0 - 1e-15));
-        if (csum > 0.0) { cp *= x_c_total / csum; co *= x_c_total / csum; }
-        cp = dmax(cp, 1e-30 * x_c_total);
-        co = dmax(co, 1e-30 * x_c_total);
-        if (cp + co >= x_c_total) { double s = (1.0 - 1e-12) * x_c_total / (cp + co); cp *= s; co *= s; }
-        y[0] = h; y[1] = cp; y[2] = co;
-        st = chem_steady_cell(p, x_c_total, x_hcop[i], y, max_iter, rtol, dt0, growth, &itc);
+        memset(&p, 0, sizeof(p));
+        p.n_h = n_h[i]; p.kci = k_ci[i]; p.acp = alpha_cp[i]; p.rh2 = r_h2_half_nh[i];
+        p.rcr = r_cr_base[i]; p.xc = x_c_total; p.hcop = x_hcop[i];
+        if (u_h2) {
+            p.ss = 1; p.kpd0 = k_pd_base[i]; p.kco0 = k_co_total[i]; p.kco_cr = kco_cr[i];
+            p.u_h2 = u_h2[i]; p.u_co = u_co[i]; p.ds = ds[i]; p.b_dop = b_dop;
+            p.ds_co = co_implicit ? ds[i] : 0.0;
+        } else {
+            p.kpd = k_pd_base[i]; p.kco = k_co_total[i];
+        }
+        for (k = 0; k < 5; ++k) y[k] = dmax(y[k], 1e-30);
+        st = chem_steady_cell(&p, y, max_iter, rtol, growth, &itc, fo);
         if (iters) iters[i] = itc;
         if (status) status[i] = st;
+        if (fsh) { fsh[i] = fo[0]; fsh[n + i] = fo[1]; }
         if (st == 0) nconv += 1;
-        x_h2[i] = y[0];
-        x_hi[i] = 1.0 - 2.0 * y[0];
-        x_cp[i] = y[1];
-        x_co[i] = y[2];
-        x_c[i] = x_c_total - y[1] - y[2];
-        x_o[i] = dmax(X_O_TOTAL - y[2], 1e-30);
-        x_e[i] = dmax(y[1] + x_hcop[i], 1e-30);
+        x_hi[i] = y[0]; x_h2[i] = y[1]; x_cp[i] = y[2]; x_c[i] = y[3]; x_co[i] = y[4];
+        x_o[i] = dmax(X_O_TOTAL - y[4], 1e-30);
+        x_e[i] = dmax(y[2] + x_hcop[i], 1e-30);
     }
     return nconv;
 }
 
-/* Bisection (thermal.rs:231-243) then safeguarded Newton polish with a
- * central-free forward-difference slope until |dT| <= tol * T. */
+/* Bisection (thermal.rs:231-243) then a safeguarded Newton polish with a
+ * forward-difference slope until |dT| <= tol T or the bracket is narrower
+ * than tol T (a sign change at one of the net-heating discontinuities --
+ * the CO ladder break, T = 100 K, T = 3000 K -- converges to the jump). */
 static double thermal_root_cell(const thermal_ctx_t *c, const double *cii, const double *oi63,
                                 const double *oi145, const double *ci, int64_t n_bisect,
                                 int64_t max_newton, double tol, int64_t *iters, int *status) {
-    double t_lo = 10.0, t_hi = 1e5, t;
+    double t_lo = 10.0, t_hi = 1e5, t, dx_old, dx;
     int64_t k;
     *status = 1;
     for (k = 0; k < n_bisect; ++k) {
@@ -580,18 +664,30 @@ static double thermal_root_cell(const thermal_ctx_t *c, const double *cii, const
         double net = net_heating(t_mid, c, cii, oi63, oi145, ci);
         if (net > 0.0) t_lo = t_mid; else t_hi = t_mid;
     }
+    /* Safeguarded Newton (bisection whenever the Newton step leaves the
+     * bracket or does not at least halve the previous step), net > 0 below
+     * the root. */
     t = sqrt(t_lo * t_hi);
+    dx_old = t_hi - t_lo;
+    dx = dx_old;
     for (k = 0; k < max_newton; ++k) {
         double f = net_heating(t, c, cii, oi63, oi145, ci);
-        double eps, fp, dfdt, dt;
-        if (f > 0.0) t_lo = dmax(t_lo, t); else t_hi = dmin(t_hi, t);
-        eps = t * 1e-6;
-        fp = net_heating(t + eps, c, cii, oi63, oi145, ci);
-        dfdt = (fp - f) / eps;
-        dt = (fabs(dfdt) > 1e-300) ? -f / dfdt : 0.0;
-        if (!(t + dt > t_lo && t + dt < t_hi)) dt = 0.5 * (t_lo + t_hi) - t; /* bisect */
-        t += dt;
-        if (fabs(dt) <= tol * t || t_hi - t_lo <= tol * t) { *status = 0; ++k; break; }
+        double eps = t * 1e-7;
+        double df = (net_heating(t + eps, c, cii, oi63, oi145, ci) - f) / eps;
+        double tn;
+        if (f > 0.0) t_lo = t; else t_hi = t;
+        if (f == 0.0) { *status = 0; ++k; break; }
+        tn = t - f / df;
+        if (!(df != 0.0) || !(tn > t_lo && tn < t_hi) || fabs(2.0 * f) > fabs(dx_old * df)) {
+            dx_old = dx;
+            tn = 0.5 * (t_lo + t_hi);
+            dx = tn - t;
+        } else {
+            dx_old = dx;
+            dx = tn - t;
+        }
+        t = tn;
+        if (fabs(dx) <= tol * t || t_hi - t_lo <= tol * t) { *status = 0; ++k; break; }
     }
     *iters = k;
     return t;

@@ -163,6 +163,90 @@ int p3d_fuv_field_3d_dev(int64_t nx, int64_t ny, int64_t nz, const double *densi
                          double *n_h_col, double *n_h2_col, double *n_co_col,
                          int32_t *ray_out, void *stream);
 
+/* ---------------------------------------------------------------------
+ * Device-resident steady-state driver (the new method on the reference's
+ * equations; the outer loop of prism3d/solver_3d.py:197-459 with the
+ * per-iteration physics of :262-376).  One handle holds one grid on the
+ * current device.  No counterpart entry point in the reference: its
+ * PDRSolver3D.run() reaches the same kernels through the three functions
+ * above.
+ *
+ * p3d_steady_create  copy density, ray set, PE table and line data to the
+ *                    device (host pointers); x_c_total / x_o_total are the
+ *                    gas-phase C and O abundances, t_init the initial T_gas,
+ *                    h2_sigmas the THEMIS H2-formation area sums (nano,
+ *                    large carbon, silicate; themis_tables.py:255-276).
+ * p3d_steady_reset   full ray march (G0, A_V, N_H, selected ray), per-cell
+ *                    constants and the analytic initial abundances
+ *                    (solver_3d.py:155-191).
+ * p3d_steady_run     up to max_outer outer iterations until the relative
+ *                    change of T_gas and of every species above 1e-20
+ *                    exceeds tol in at most n_allow cells (n_allow = 0: in
+ *                    none; a few cells sit on a discontinuity of the
+ *                    reference's thermal balance and settle slowly).
+ *                    mixed = 0: FP64 throughout, one
+ *                    host check per iteration; mixed = 1: FP32 factorisation
+ *                    and bisection with FP64 residuals, certificates and
+ *                    polish, warm starts, cells that reached their fixed
+ *                    point skipped until their inputs move, iterations
+ *                    replayed from a CUDA graph.
+ *                    w_chem damps the abundances (convex combination of old
+ *                    and new), w_t is the damping of the per-cell T update
+ *                    before a fixed point is bracketed.  Returns
+ *                    P3D_ECONVERGE (state kept) if tol was not reached.
+ * p3d_steady_get     copy one per-cell field (P3D_F_*) to host memory.
+ * p3d_steady_history (largest relative change, chemistry failures, thermal
+ *                    failures) per iteration since the last reset.
+ * ------------------------------------------------------------------- */
+typedef struct p3d_steady p3d_steady_t;
+
+#define P3D_F_T_GAS 0
+#define P3D_F_X_HI 1
+#define P3D_F_X_H2 2
+#define P3D_F_X_CP 3
+#define P3D_F_X_C 4
+#define P3D_F_X_CO 5
+#define P3D_F_X_O 6
+#define P3D_F_X_E 7
+#define P3D_F_G0 8
+#define P3D_F_A_V 9
+#define P3D_F_N_H 10
+#define P3D_F_N_H2 11
+#define P3D_F_N_CO 12
+#define P3D_F_T_DUST 13
+#define P3D_F_GAMMA_PE 14
+#define P3D_F_ZETA 15
+#define P3D_F_F_SH_H2 16
+
+int p3d_steady_create(p3d_steady_t **out, int64_t nx, int64_t ny, int64_t nz,
+                      const double *density, const double *g0_ext, int64_t n_g0,
+                      double cell_size, const double *dirs, const double *weights,
+                      int64_t n_rays, double zeta0, double x_c_total, double x_o_total,
+                      double t_init, const double *pe_table, int64_t n_bins, double log_psi_min,
+                      double log_psi_step, int64_t n_psi, double eg_min, double eg_step,
+                      int64_t n_eg, const double *bin_sigma_abs, const double *bin_dn_da_da,
+                      const double *bin_is_nano, const double *h2_sigmas, const double *cii,
+                      const double *oi63, const double *oi145, const double *ci);
+int p3d_steady_reset(p3d_steady_t *s);
+int p3d_steady_run(p3d_steady_t *s, int mixed, int64_t max_outer, double tol, int64_t n_allow,
+                   double w_chem, double w_t, int64_t *iters_out, double *dmax_out);
+int p3d_steady_get(p3d_steady_t *s, int field, double *host_out);
+int p3d_steady_get_ray(p3d_steady_t *s, int32_t *host_out);
+/* 9 doubles per iteration: largest relative change, chemistry and thermal
+ * failures, cells changing more than 100 tol / tol / tol / 100, FP64
+ * net-heating evaluations, grid-mean T, cells solved. */
+int p3d_steady_history(p3d_steady_t *s, double *out, int64_t max_n, int64_t *n_out);
+int p3d_steady_destroy(p3d_steady_t *s);
+/* Device time (CUDA events on the library stream) from the start of the
+ * last p3d_steady_reset to the end of the last p3d_steady_run. */
+int p3d_steady_elapsed_ms(p3d_steady_t *s, double *ms);
+/* Kernels launched on the device since the last p3d_steady_reset. */
+int p3d_steady_launch_count(p3d_steady_t *s, int64_t *out);
+/* Mean time (ms) over reps launches on the current state of: the three
+ * selected-ray column passes, the grid-mean T reduction, the mixed and the
+ * plain per-cell kernel with every cell solved.  Advances the state. */
+int p3d_steady_kernel_times(p3d_steady_t *s, int reps, double *ms4);
+
 #ifdef __cplusplus
 }
 #endif

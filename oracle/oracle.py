@@ -171,7 +171,8 @@ def pe_heating_vec(pe_table, log_psi_min, log_psi_step, n_psi, eg_min, eg_step, 
 
 def chem_steady(n_h, k_pd_base, k_ci, alpha_cp, k_co_total, r_h2_half_nh, r_cr_base,
                 x_c_total, x_hi, x_h2, x_cp, x_c, x_co, x_o, x_e, x_hcop,
-                max_iter=200, rtol=1e-12, growth=4.0, selfshield=None, co_implicit=False):
+                max_iter=200, rtol=1e-12, growth=4.0, selfshield=None, co_implicit=False,
+                h2_implicit=False):
     """FP64 backward-Euler/Newton steady state of the reduced network (new
     method on the equations of rust/src/chemistry.rs:35-49).  In place.
 
@@ -192,10 +193,11 @@ def chem_steady(n_h, k_pd_base, k_ci, alpha_cp, k_co_total, r_h2_half_nh, r_cr_b
         ss = [_f64(a) for a in (kcr, uh2, uco, ds)]
         fsh = np.zeros(2 * n)
         extra = [*[_p(a) for a in ss], ctypes.c_double(b), ctypes.c_int(int(co_implicit)),
-                 _p(fsh)]
+                 ctypes.c_int(int(h2_implicit)), _p(fsh)]
     else:
         fsh = None
-        extra = [None, None, None, None, ctypes.c_double(0.0), ctypes.c_int(0), None]
+        extra = [None, None, None, None, ctypes.c_double(0.0), ctypes.c_int(0), ctypes.c_int(0),
+                 None]
     r = f(ctypes.c_int64(n), *[_p(a) for a in ins[:7]], ctypes.c_double(x_c_total),
           *[_p(a) for a in st], _p(ins[7]), ctypes.c_int64(max_iter), ctypes.c_double(rtol),
           ctypes.c_double(growth), *extra, iters.ctypes.data_as(_I64),
@@ -578,16 +580,17 @@ def t_update(T_in, G, mem, w_T=0.5):
 def steady_run(density, G0_external, cell_size, nside=1, zeta0=2e-16, T_init=100.0,
                max_outer=500, tol=1e-10, w_chem=0.5, w_T=0.5, chem_rtol=1e-12,
                therm_tol=1e-12, tables=None, lines=None, verbose=False, callback=None,
-               co_implicit=False):
+               co_implicit=False, h2_implicit=False, accel=False):
     """FP64 CPU restatement of the GPU steady-state driver.
 
     Outer fixed-point iteration with the per-iteration physics of
     PDRSolver3D.run() (solver_3d.py:262-376): columns along each cell's
     selected ray -> shielding / CR / dust -> chemistry -> thermal balance.
-    Chemistry is solved to F(x) = 0 (backward-Euler / Newton) with the
-    cell's own half layer in its H2 and CO shielding columns solved
-    implicitly; abundances are damped by w_chem (convex combination of the
-    old and new conserved states); T follows the per-cell bracketed secant
+    Chemistry is solved to F(x) = 0 (backward-Euler / Newton in relative
+    variables) with the shielding columns of the start of the iteration
+    (h2_implicit / co_implicit solve the cell's own half layer implicitly
+    instead); abundances are damped by w_chem (convex combination of the old
+    and new conserved states); T follows the per-cell bracketed secant
     update of t_update() on the thermal root (bisection + safeguarded
     Newton).  Stops when the largest relative change of T and of every
     species above 1e-20 (relative to n_H) is below tol.
@@ -613,11 +616,13 @@ def steady_run(density, G0_external, cell_size, nside=1, zeta0=2e-16, T_init=100
     hist = []
     mem = (np.zeros(shp), np.zeros(shp), np.zeros(shp), np.full(shp, np.inf),
            np.full(shp, np.inf))
+    amem = None
+    accel_clip = 4.0
     for it in range(max_outer):
         old = {k: st[k].copy() for k in ("T_gas",) + species}
         NH2, NCO = selected_columns(n, st["x_H2"], st["x_CO"], ray, dirs, cell_size)
         st["N_H2"], st["N_CO"] = NH2, NCO
-        u_h2 = NH2 - n * st["x_H2"] * ds
+        u_h2 = NH2 - n * st["x_H2"] * ds if h2_implicit else NH2
         u_co = NCO - 0.5 * n * st["x_CO"] * ds if co_implicit else NCO
         t_mean = np.mean(st["T_gas"])
         b_dop = np.sqrt(2.0 * k_boltz * t_mean / m_H2) / 1e5
@@ -628,10 +633,27 @@ def steady_run(density, G0_external, cell_size, nside=1, zeta0=2e-16, T_init=100
         _, iters, status, fsh = chem_steady(
             n, const["kpd0"], const["kci"], a_cp, const["kco0"], st["R_H2"] * n * 0.5,
             2.5 * const["zeta"] * 0.1, X_C, *xs, st["x_HCOp"], rtol=chem_rtol,
-            selfshield=(6.0 * const["zeta"], u_h2, u_co, ds, b_dop), co_implicit=co_implicit)
+            selfshield=(6.0 * const["zeta"], u_h2, u_co, ds, b_dop), co_implicit=co_implicit,
+            h2_implicit=h2_implicit)
         for k, a in zip(species + ("x_O", "x_e"), xs):
             st[k] = a.reshape(shp)
-        if it > 0 and w_chem > 0:
+        if accel:
+            z_old = _zvars(old)
+            z_new = _zvars(st)
+            r = z_new - z_old
+            if it > 0:
+                dr = r - amem[1]
+                dz = z_old - amem[0]
+                num = np.sum(dr * r, axis=0)
+                den = np.sum(dr * dr, axis=0)
+                gam = np.where(den > 0, num / np.where(den > 0, den, 1.0), 0.0)
+                gam = np.clip(gam, -accel_clip, accel_clip)
+                z = z_old + (1 - w_chem) * r - gam * (dz + (1 - w_chem) * dr)
+            else:
+                z = z_old + (1 - w_chem) * r
+            amem = (z_old, r)
+            _from_zvars(st, z)
+        elif it > 0 and w_chem > 0:
             for k in species:
                 st[k] = w_chem * old[k] + (1.0 - w_chem) * st[k]
         f_h2 = fsh[0].reshape(shp)
@@ -653,3 +675,19 @@ def steady_run(density, G0_external, cell_size, nside=1, zeta0=2e-16, T_init=100
         if dmax < tol and it > 1:
             break
     return st, hist
+
+
+def _zvars(st):
+    """Log-ratio coordinates of the conserved abundance vector."""
+    return np.stack([np.log(st["x_H2"] / st["x_HI"]), np.log(st["x_CO"] / st["x_Cp"]),
+                     np.log(st["x_C"] / st["x_Cp"])])
+
+
+def _from_zvars(st, z):
+    rho = np.exp(z[0])
+    st["x_HI"] = 1.0 / (1.0 + 2.0 * rho)
+    st["x_H2"] = rho / (1.0 + 2.0 * rho)
+    r1, r2 = np.exp(z[1]), np.exp(z[2])
+    st["x_Cp"] = X_C / (1.0 + r1 + r2)
+    st["x_CO"] = r1 * st["x_Cp"]
+    st["x_C"] = r2 * st["x_Cp"]

@@ -428,7 +428,8 @@ void or_pe_heating_vec(const double *table, int64_t n_bins, double log_psi_min,
  * backward-Euler steps on rows 0, 2, 3 ((1/dt) dy - J dy = f) with the
  * constraints imposed exactly, dt growing by `growth` per accepted step and
  * shrinking on a non-positive iterate, until every |dy_i| <= rtol y_i and
- * every rate residual <= rtol of its largest production/destruction term.
+ * every rate residual <= rtol of its production + destruction.  The linear
+ * systems are solved for relative changes dy_i / y_i (columns scaled by y).
  * status 0 = converged, 1 = iteration limit.
  */
 typedef struct {
@@ -439,6 +440,7 @@ typedef struct {
     int ss;
     double kpd0, kco0, kco_cr, u_h2, u_co, ds, ds_co, b_dop;
 } chem_par_t;
+/* ds is the own-layer factor of N_H2 (0: the whole column is in u_h2). */
 
 /* f_shield_H2 (shielding.py:17-59) and d f / d N. */
 static double fsh_h2(double n, double b, double *dfdn) {
@@ -561,6 +563,9 @@ static const int kOdeRow[5] = {1, -1, 2, 4, -1}; /* row -> species it advances *
  * residual <= rtol of its production + destruction. */
 static int chem_steady_cell(const chem_par_t *p, double *y, int64_t max_iter, double rtol,
                             double growth, int64_t *iters_out, double *fsh_out) {
+    /* Newton / PTC in relative variables: columns are scaled by y, the
+     * unknowns are w = dy / y, so a species many orders below its element
+     * total is still resolved to relative precision. */
     double inv_dt = 0.0;
     int64_t it;
     int status = 1;
@@ -577,11 +582,12 @@ static int chem_steady_cell(const chem_par_t *p, double *y, int64_t max_iter, do
                 for (c = 0; c < 5; ++c) A[r][c] = J[r][c];
                 d[r] = -f[r];
             }
+            for (c = 0; c < 5; ++c) A[r][c] *= y[c];
         }
         if (solve5(A, d)) ok = 0;
         for (r = 0; ok && r < 5; ++r) {
-            yn[r] = y[r] + d[r];
-            if (!(yn[r] > 0.0)) ok = 0;
+            if (!(d[r] > -1.0)) ok = 0;
+            yn[r] = y[r] * (1.0 + d[r]);
         }
         if (!ok) {
             double lam = 0.0;
@@ -590,7 +596,7 @@ static int chem_steady_cell(const chem_par_t *p, double *y, int64_t max_iter, do
             continue;
         }
         for (r = 0; r < 5; ++r) {
-            if (fabs(d[r]) > rtol * dmax(yn[r], 1e-20)) conv = 0;
+            if (fabs(d[r]) > rtol) conv = 0;
             if (kOdeRow[r] >= 0 && fabs(f[r]) > rtol * sc[r]) conv = 0;
         }
         for (r = 0; r < 5; ++r) y[r] = yn[r];
@@ -617,7 +623,7 @@ int64_t or_chem_steady(int64_t n, const double *n_h, const double *k_pd_base, co
                        double *x_o, double *x_e, const double *x_hcop, int64_t max_iter,
                        double rtol, double growth, const double *kco_cr, const double *u_h2,
                        const double *u_co, const double *ds, double b_dop, int co_implicit,
-                       double *fsh, int64_t *iters, int32_t *status) {
+                       int h2_implicit, double *fsh, int64_t *iters, int32_t *status) {
     int64_t i, nconv = 0;
 #pragma omp parallel for schedule(dynamic, 1024) reduction(+ : nconv)
     for (i = 0; i < n; ++i) {
@@ -631,7 +637,8 @@ int64_t or_chem_steady(int64_t n, const double *n_h, const double *k_pd_base, co
         p.rcr = r_cr_base[i]; p.xc = x_c_total; p.hcop = x_hcop[i];
         if (u_h2) {
             p.ss = 1; p.kpd0 = k_pd_base[i]; p.kco0 = k_co_total[i]; p.kco_cr = kco_cr[i];
-            p.u_h2 = u_h2[i]; p.u_co = u_co[i]; p.ds = ds[i]; p.b_dop = b_dop;
+            p.u_h2 = u_h2[i]; p.u_co = u_co[i]; p.b_dop = b_dop;
+            p.ds = h2_implicit ? ds[i] : 0.0;
             p.ds_co = co_implicit ? ds[i] : 0.0;
         } else {
             p.kpd = k_pd_base[i]; p.kco = k_co_total[i];

@@ -39,6 +39,18 @@ SIGNATURES = {
                         [_I32],
     "p3d_fuv_field_3d_dev": [_i64, _i64, _i64, _D, _D, _D, _D, _i64, _f64, _D, _D, _i64] +
                             [_D] * 5 + [_I32, _vp],
+    "p3d_steady_create": [ctypes.POINTER(_vp), _i64, _i64, _i64, _D, _D, _i64, _f64, _D, _D, _i64,
+                          _f64, _f64, _f64, _f64, _D, _i64, _f64, _f64, _i64, _f64, _f64, _i64,
+                          _D, _D, _D, _D, _D, _D, _D, _D],
+    "p3d_steady_reset": [_vp],
+    "p3d_steady_run": [_vp, ctypes.c_int, _i64, _f64, _i64, _f64, _f64, _I64, _D],
+    "p3d_steady_get": [_vp, ctypes.c_int, _D],
+    "p3d_steady_get_ray": [_vp, _I32],
+    "p3d_steady_history": [_vp, _D, _i64, _I64],
+    "p3d_steady_destroy": [_vp],
+    "p3d_steady_launch_count": [_vp, _I64],
+    "p3d_steady_elapsed_ms": [_vp, _D],
+    "p3d_steady_kernel_times": [_vp, ctypes.c_int, _D],
 }
 _RESTYPES = {"p3d_version": ctypes.c_char_p, "p3d_last_error": ctypes.c_char_p}
 

@@ -44,7 +44,7 @@ int cuda_fail(cudaError_t e, const char* where) {
 static std::mutex g_mu;
 static std::vector<DeviceState*> g_states;
 
-static void co_ladder_host(CoLevel* out) {
+void co_ladder_host(CoLevel* out) {
   // rust/src/thermal.rs:21-41 (same operation order)
   const double B = 57.635968e9, mu = 0.1098e-18, c = 2.99792458e10, pi = 3.14159265358979323846;
   for (int ju = 1; ju <= 40; ++ju) {

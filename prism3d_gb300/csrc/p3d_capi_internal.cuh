@@ -33,6 +33,7 @@ int set_error(int code, const char* fmt, ...);
 int cuda_fail(cudaError_t e, const char* where);
 int get_state(DeviceState** out);
 int sync_check(cudaStream_t s, const char* where);
+void co_ladder_host(CoLevel* out);
 int build_rayset(const double* dirs, const double* weights, int64_t n_rays,
                  const double* g0_ext, int64_t n_g0, double cell_size, RaySet* rs);
 

@@ -1,0 +1,82 @@
+// p3d_phys.cuh -- per-cell physics used by the steady-state driver (FP64).
+#pragma once
+
+#include "p3d_common.cuh"
+
+namespace p3d {
+
+constexpr double kMH = 1.6735575e-24;
+constexpr double kPi = 3.14159265358979323846;
+
+// f_shield_H2, Draine & Bertoldi 1996 (radiative_transfer/shielding.py:17-59)
+// with b the Doppler parameter in km/s; *dfdn = d f / d N_H2 (0 where the
+// clip to [0, 1] is active).
+__device__ __forceinline__ double fsh_h2(double n, double b, double* dfdn) {
+  double x = n / 5.0e14;
+  double q = 1.0 + x / b;
+  double sq = sqrt(1.0 + x);
+  double e = exp(-8.5e-4 * sq);
+  double f = 0.965 / (q * q) + 0.035 / sq * e;
+  double d = -2.0 * 0.965 / (q * q * q) / b +
+             0.035 * e * (-0.5 / ((1.0 + x) * sq) - 0.5 * 8.5e-4 / (1.0 + x));
+  *dfdn = (f > 0.0 && f < 1.0) ? d / 5.0e14 : 0.0;
+  return fmin(fmax(f, 0.0), 1.0);
+}
+
+// f_shield_CO (shielding.py:136-171) and its N_H2 derivative.
+__device__ __forceinline__ double fsh_co(double nco_in, double nh2_in, double* d_h2) {
+  double nco = fmax(nco_in, 1.0), nh2 = fmax(nh2_in, 1.0);
+  double A = 6.428e-8 * pow(nco, 0.53);
+  double B = 3.0e-12 * pow(nh2, 0.495);
+  double Cc = 1e-5 * pow(nco, 0.6);
+  double P4 = pow(nh2, 0.48);
+  double E = exp(-8e-12 * P4);
+  double f = exp(-A) * exp(-B) * (1.0 / (1.0 + Cc * E));
+  bool live = (f > 1e-10 && f < 1.0);
+  *d_h2 = (live && nh2_in > 1.0)
+              ? f * (-0.495 * B / nh2 + Cc * E * 8e-12 * 0.48 * P4 / (nh2 * (1.0 + Cc * E)))
+              : 0.0;
+  return fmin(fmax(f, 1e-10), 1.0);
+}
+
+// Padovani et al. model 'M' (cosmic_rays/attenuation.py:18-113).
+__device__ __forceinline__ double padovani(double nh, double a0, double a1, double a2,
+                                           double b0, double b1, double deep) {
+  double x = log10(fmax(nh, 1e18) / 1e20);
+  double lz = x < -1.0 ? a0 : (x < 2.0 ? a0 - a1 * x - a2 * x * x
+                                      : (x < 5.0 ? b0 - b1 * (x - 2.0) : deep));
+  return pow(10.0, lz);
+}
+
+__device__ __forceinline__ double cr_rate(double nh, double zeta0) {
+  double zl = padovani(nh, -15.7, 0.4, 0.1, -16.3, 0.8, -18.7);
+  double zh = padovani(nh, -15.0, 0.35, 0.08, -15.6, 0.7, -17.7);
+  return fmax(sqrt(zl * zh) * (zeta0 / 2e-16), 1e-22);
+}
+
+// Radiative part of the THEMIS dust temperature (themis_tables.py:333-342).
+__device__ __forceinline__ double tdust_rad(double g0, double av) {
+  double F = kFHabing * g0 * exp(-1.8 * av);
+  F = F + kFHabing * 0.5 * exp(-av);
+  F = fmax(F, 1e-30);
+  return fmin(fmax(16.4 * pow(F / kFHabing, 0.167), 5.0), 200.0);
+}
+
+// Gas-grain coupling at high density (themis_tables.py:344-352).
+__device__ __forceinline__ double tdust(double td_rad, double nh, double tg) {
+  double fc = fmin(fmax(nh / 1e7, 0.0), 1.0);
+  return nh > 1e5 ? td_rad * (1.0 - fc) + tg * fc : td_rad;
+}
+
+// H2 formation rate coefficient (themis_tables.py:278-319).
+__device__ __forceinline__ double h2_form(double tg, double td, double fnano, double s_nano,
+                                          double s_lc, double s_sil) {
+  double v = sqrt(8.0 * kKBoltz * tg / (kPi * kMH));
+  double s = 1.0 / (1.0 + 0.04 * sqrt(tg + td) + 0.002 * tg + 8e-6 * tg * tg);
+  double e_sil = td < 14.0 ? 1.0 : (td < 25.0 ? exp(-(td - 14.0) / 5.0) : 0.01);
+  double e_c = td < 50.0 ? 0.8 : (td < 400.0 ? 0.8 * exp(-(td - 50.0) / 200.0) : 0.01);
+  e_c = fmax(e_c, 0.005);
+  return 0.5 * v * s * (e_c * s_nano * fnano + e_c * s_lc + e_sil * s_sil);
+}
+
+}  // namespace p3d

@@ -1,0 +1,482 @@
+// p3d_steady.cu -- device-resident steady-state driver (kernels in
+// p3d_steady_kernels.cuh) and its host runtime behind the C ABI.
+//
+// Owns the per-cell device arrays of one grid, the library stream and, for
+// the mixed path, a CUDA graph holding `kGraphIters` outer iterations that
+// is relaunched until the convergence history read back after each launch
+// drops below the tolerance.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/prism3d_gb300.h"
+#include "p3d_capi_internal.cuh"
+#include "p3d_common.cuh"
+#include "p3d_pe.cuh"
+#include "p3d_rt.cuh"
+#include "p3d_steady.cuh"
+#include "p3d_steady_kernels.cuh"
+
+namespace p3d {
+
+constexpr int kGraphIters = 8;
+constexpr int kMaxHist = 1 << 16;
+
+struct SteadySolver {
+  DeviceState* st = nullptr;
+  int64_t nx = 0, ny = 0, nz = 0, n = 0;
+  RaySet rays;
+  SteadyParams par;
+  SteadyDev d;
+  std::vector<void*> allocs;
+  double* dens = nullptr;
+  double *nh2_full = nullptr, *nco_full = nullptr, *scratch = nullptr;
+  double *a_nano = nullptr, *a_rest = nullptr;
+  double *ray_ds = nullptr;
+  int* ray_fam = nullptr;
+  double* parts = nullptr;
+  int nparts = 0;
+  SteadyGlobals* glob = nullptr;
+  double* hist = nullptr;
+  double* hist_host = nullptr;  // pinned
+  cudaGraphExec_t graph = nullptr;
+  int graph_mixed = -1;
+  SteadyParams graph_par;
+  int64_t iters_done = 0;
+  int64_t launches = 0;  // kernels launched since the last reset
+  cudaEvent_t ev_start = nullptr, ev_stop = nullptr;  // reset .. end of last run
+  double last_dmax = INFINITY;
+
+  template <typename T>
+  int alloc(T** p, size_t count) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, sizeof(T) * (count ? count : 1));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return cuda_fail(e, "steady cudaMalloc");
+    }
+    allocs.push_back(q);
+    *p = (T*)q;
+    return P3D_OK;
+  }
+
+  ~SteadySolver() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (ev_start) cudaEventDestroy(ev_start);
+    if (ev_stop) cudaEventDestroy(ev_stop);
+    if (st) cudaStreamSynchronize(st->stream);
+    for (void* q : allocs) cudaFree(q);
+    if (hist_host) cudaFreeHost(hist_host);
+  }
+};
+
+static int launch_iteration(SteadySolver* s, bool mixed, const SteadyParams& par,
+                            cudaStream_t str) {
+  const SteadyDev& d = s->d;
+  int64_t dims[3] = {s->nx, s->ny, s->nz};
+  for (int axis = 0; axis < 3; ++axis) {
+    int64_t np = s->n / dims[axis];
+    ss_columns_kernel<<<(unsigned)ceil_div(np, 128), 128, 0, str>>>(
+        axis, par.h2_implicit, s->nx, s->ny, s->nz, np, s->dens, d.x_h2, d.x_co, d.fam, d.ds,
+        d.u_h2, d.u_co);
+  }
+  ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(s->n, d.t_gas, s->parts);
+  ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, s->n, s->glob);
+  unsigned grid = grid_for(s->n, s->st->sms, 4);
+  if (mixed)
+    ss_cell_kernel<true><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->glob,
+                                                     s->a_nano, s->a_rest);
+  else
+    ss_cell_kernel<false><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->glob,
+                                                      s->a_nano, s->a_rest);
+  ss_record_kernel<<<1, 32, 0, str>>>(s->glob, s->hist, kMaxHist);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? P3D_OK : cuda_fail(e, "steady iteration launch");
+}
+
+constexpr int kLaunchesPerIteration = 7;
+
+}  // namespace p3d
+
+using namespace p3d;
+
+struct p3d_steady {
+  SteadySolver s;
+};
+
+extern "C" {
+
+int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
+                      const double* density, const double* g0_ext, int64_t n_g0,
+                      double cell_size, const double* dirs, const double* weights,
+                      int64_t n_rays, double zeta0, double x_c_total, double x_o_total,
+                      double t_init, const double* pe_table, int64_t n_bins, double log_psi_min,
+                      double log_psi_step, int64_t n_psi, double eg_min, double eg_step,
+                      int64_t n_eg, const double* bin_sigma_abs, const double* bin_dn_da_da,
+                      const double* bin_is_nano, const double* h2_sigmas, const double* cii,
+                      const double* oi63, const double* oi145, const double* ci) {
+  if (!out) return set_error(P3D_EINVAL, "null handle pointer");
+  *out = nullptr;
+  DeviceState* st;
+  int rc = get_state(&st);
+  if (rc) return rc;
+  if (nx <= 0 || ny <= 0 || nz <= 0) return set_error(P3D_EINVAL, "grid must be non-empty");
+  if (!density || !g0_ext || !dirs || !weights || !pe_table || !bin_sigma_abs ||
+      !bin_dn_da_da || !bin_is_nano || !h2_sigmas || !cii || !oi63 || !oi145 || !ci)
+    return set_error(P3D_EINVAL, "null argument");
+  if (n_psi < 2 || n_eg < 2 || n_bins < 1) return set_error(P3D_EINVAL, "bad PE table shape");
+  p3d_steady* h = new p3d_steady();
+  SteadySolver* s = &h->s;
+  s->st = st;
+  s->nx = nx; s->ny = ny; s->nz = nz; s->n = nx * ny * nz;
+  const int64_t n = s->n;
+  if ((rc = build_rayset(dirs, weights, n_rays, g0_ext, n_g0, cell_size, &s->rays))) {
+    delete h;
+    return rc;
+  }
+  SteadyParams& p = s->par;
+  p.zeta0 = zeta0; p.x_c_total = x_c_total; p.x_o_total = x_o_total; p.x_hcop = 1e-10;
+  p.t_init = t_init; p.f_nano = 1.0; p.e_g = 0.1;
+  p.sigma_nano = h2_sigmas[0]; p.sigma_lc = h2_sigmas[1]; p.sigma_sil = h2_sigmas[2];
+  p.w_chem = 0.5; p.w_t = 0.5; p.chem_rtol = 1e-12; p.therm_tol = 1e-12;
+  p.chem_max_iter = 200; p.therm_max_iter = 80; p.n_rays = (int)n_rays;
+  p.h2_implicit = 0;
+  p.pe = PeGrid{log_psi_min, log_psi_step, eg_min, eg_step, (int)n_psi, (int)n_eg};
+  memcpy(p.lines.cii, cii, sizeof(p.lines.cii));
+  memcpy(p.lines.oi63, oi63, sizeof(p.lines.oi63));
+  memcpy(p.lines.oi145, oi145, sizeof(p.lines.oi145));
+  memcpy(p.lines.ci, ci, sizeof(p.lines.ci));
+  SteadyDev& d = s->d;
+  double** dbl[] = {&s->dens, &d.g0, &d.av, &d.nh_col, &s->nh2_full, &s->nco_full, &d.ds,
+                    &d.kpd0, &d.uv0, &d.kci, &d.kco0, &d.hci0, &d.zeta, &d.td_rad, &d.t_gas,
+                    &d.x_hi, &d.x_h2, &d.x_cp, &d.x_c, &d.x_co, &d.x_o, &d.x_e, &d.u_h2,
+                    &d.u_co, &d.t_prev, &d.r_prev, &d.t_lo, &d.t_hi, &d.span, &d.t_root, &d.u_h2_last, &d.u_co_last, &d.b_last, &d.chg_last, &d.fh2,
+                    &d.gamma_pe, &d.t_dust, &s->scratch};
+  for (double** q : dbl)
+    if ((rc = s->alloc(q, n))) { delete h; return rc; }
+  d.dens = s->dens;
+  if ((rc = s->alloc(&d.ray, n)) || (rc = s->alloc(&d.fam, n)) || (rc = s->alloc(&d.flags, n))) {
+    delete h;
+    return rc;
+  }
+  size_t npe = (size_t)n_psi * n_eg;
+  double *tab = nullptr, *bins = nullptr;
+  if ((rc = s->alloc(&s->a_nano, 2 * npe)) || (rc = s->alloc(&tab, npe * n_bins)) ||
+      (rc = s->alloc(&bins, 3 * n_bins)) || (rc = s->alloc(&s->ray_ds, n_rays)) ||
+      (rc = s->alloc(&s->ray_fam, n_rays))) {
+    delete h;
+    return rc;
+  }
+  s->a_rest = s->a_nano + npe;
+  s->nparts = 2 * st->sms;
+  if ((rc = s->alloc(&s->parts, s->nparts)) || (rc = s->alloc(&s->glob, 1)) ||
+      (rc = s->alloc(&s->hist, kHistCols * (size_t)kMaxHist))) {
+    delete h;
+    return rc;
+  }
+  cudaError_t e = cudaMallocHost(&s->hist_host, sizeof(double) * kHistCols * kMaxHist);
+  if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaMallocHost"); }
+  cudaStream_t str = st->stream;
+  std::vector<double> hb(3 * n_bins), hds(n_rays);
+  std::vector<int> hfam(n_rays);
+  for (int64_t b = 0; b < n_bins; ++b) {
+    hb[b] = bin_sigma_abs[b];
+    hb[n_bins + b] = bin_dn_da_da[b];
+    hb[2 * n_bins + b] = bin_is_nano[b];
+  }
+  for (int64_t r = 0; r < n_rays; ++r) {
+    hds[r] = s->rays.ds[r];
+    hfam[r] = s->rays.axis[r] * 2 + s->rays.fwd[r];
+  }
+  {
+    CoLevel co[40];
+    co_ladder_host(co);
+    p.theta2 = co[0].t_u;
+    float l32[20], co32[200];
+    const double* L[5] = {p.lines.cii, p.lines.oi63, p.lines.oi145, p.lines.ci, p.lines.ci + 5};
+    for (int k = 0; k < 5; ++k) {
+      l32[4 * k] = (float)L[k][1];
+      l32[4 * k + 1] = (float)L[k][2];
+      l32[4 * k + 2] = (float)(L[k][3] / L[k][4]);
+      l32[4 * k + 3] = (float)L[k][4];
+    }
+    for (int k = 0; k < 40; ++k) {
+      co32[5 * k] = (float)co[k].t_u;
+      co32[5 * k + 1] = (float)co[k].a_co;
+      co32[5 * k + 2] = (float)co[k].g_ratio;
+      co32[5 * k + 3] = (float)co[k].j_factor;
+      co32[5 * k + 4] = (float)(co[k].ahv / co[0].ahv);
+    }
+    e = cudaMemcpyToSymbolAsync(c_co_ss, co, sizeof(co), 0, cudaMemcpyHostToDevice, str);
+    if (e == cudaSuccess)
+      e = cudaMemcpyToSymbolAsync(c_lines32, l32, sizeof(l32), 0, cudaMemcpyHostToDevice, str);
+    if (e == cudaSuccess)
+      e = cudaMemcpyToSymbolAsync(c_co32, co32, sizeof(co32), 0, cudaMemcpyHostToDevice, str);
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->dens, density, sizeof(double) * n, cudaMemcpyHostToDevice, str);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(tab, pe_table, sizeof(double) * npe * n_bins, cudaMemcpyHostToDevice, str);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(bins, hb.data(), sizeof(double) * hb.size(), cudaMemcpyHostToDevice, str);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->ray_ds, hds.data(), sizeof(double) * n_rays, cudaMemcpyHostToDevice, str);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->ray_fam, hfam.data(), sizeof(int) * n_rays, cudaMemcpyHostToDevice, str);
+  if (e == cudaSuccess)
+    e = launch_pe_condense(tab, (int)n_bins, p.pe, bins, bins + n_bins, bins + 2 * n_bins,
+                           s->a_nano, s->a_rest, str);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+  if (e != cudaSuccess) { delete h; return cuda_fail(e, "steady create"); }
+  *out = h;
+  return P3D_OK;
+}
+
+int p3d_steady_reset(p3d_steady_t* h) {
+  if (!h) return set_error(P3D_EINVAL, "null handle");
+  SteadySolver* s = &h->s;
+  cudaStream_t str = s->st->stream;
+  SteadyDev& d = s->d;
+  if (!s->ev_start) {
+    cudaEventCreate(&s->ev_start);
+    cudaEventCreate(&s->ev_stop);
+  }
+  cudaEventRecord(s->ev_start, str);
+  cudaError_t e = launch_fuv_full(s->nx, s->ny, s->nz, s->dens, nullptr, nullptr, s->rays, d.g0,
+                                  d.av, d.nh_col, s->nh2_full, s->nco_full, d.ray, s->st->sms,
+                                  str);
+  if (e != cudaSuccess) return cuda_fail(e, "reset: ray march");
+  ss_setup_kernel<<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(s->n, d, s->par,
+                                                                        s->ray_ds, s->ray_fam);
+  cudaMemsetAsync(d.u_h2, 0, sizeof(double) * s->n, str);
+  cudaMemsetAsync(d.u_co, 0, sizeof(double) * s->n, str);
+  ss_reset_globals_kernel<<<1, 32, 0, str>>>(s->glob);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "reset launch");
+  s->iters_done = 0;
+  int chunks = 0;
+  for (int fam = 0; fam < 6; ++fam) {
+    int cnt = 0;
+    for (int r = 0; r < s->rays.n; ++r)
+      cnt += (s->rays.axis[r] * 2 + s->rays.fwd[r] == fam);
+    chunks += (cnt + kRayChunk - 1) / kRayChunk;
+  }
+  s->launches = 2 + chunks + 2;  // ray-march init/fix, families, setup, globals
+  s->last_dmax = INFINITY;
+  return P3D_OK;
+}
+
+int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, int64_t n_allow,
+                   double w_chem, double w_t, int64_t* iters_out, double* dmax_out) {
+  if (!h) return set_error(P3D_EINVAL, "null handle");
+  if (max_outer < 0 || max_outer > kMaxHist) return set_error(P3D_EINVAL, "max_outer");
+  if (!(w_chem >= 0.0 && w_chem < 1.0) || !(w_t >= 0.0 && w_t < 1.0))
+    return set_error(P3D_EINVAL, "damping weights must lie in [0, 1)");
+  SteadySolver* s = &h->s;
+  cudaStream_t str = s->st->stream;
+  if (!(tol > 0.0) || n_allow < 0) return set_error(P3D_EINVAL, "tol must be > 0, n_allow >= 0");
+  SteadyParams par = s->par;
+  par.w_chem = w_chem;
+  par.w_t = w_t;
+  par.count_thr[0] = tol * 100.0;
+  par.count_thr[1] = tol;
+  par.count_thr[2] = tol * 0.01;
+  par.quiet_tol = tol * 0.01;
+  auto conv = [&](const double* hrow) {
+    return hrow[0] < tol || (double)hrow[4] <= (double)n_allow;
+  };
+  int64_t it = s->iters_done;
+  const int64_t stop = s->iters_done + max_outer;
+  if (stop > kMaxHist) return set_error(P3D_EINVAL, "iteration history full: reset first");
+  bool done = false;
+  cudaError_t e;
+  if (!mixed) {
+    // plain path: launch, synchronise, test -- once per iteration
+    while (it < stop && !done) {
+      int rc = launch_iteration(s, false, par, str);
+      if (rc) return rc;
+      e = cudaMemcpyAsync(s->hist_host + kHistCols * it, s->hist + kHistCols * it,
+                          sizeof(double) * kHistCols, cudaMemcpyDeviceToHost, str);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+      if (e != cudaSuccess) return cuda_fail(e, "plain iteration");
+      s->launches += kLaunchesPerIteration;
+      s->last_dmax = s->hist_host[kHistCols * it];
+      bool c = conv(s->hist_host + kHistCols * it);
+      ++it;
+      if (c && it > 2) done = true;
+    }
+  } else {
+    // mixed path: a graph of kGraphIters iterations, tested per launch
+    if (!s->graph || s->graph_mixed != 1 || memcmp(&s->graph_par, &par, sizeof(par)) != 0) {
+      if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+      cudaGraph_t g;
+      e = cudaStreamBeginCapture(str, cudaStreamCaptureModeThreadLocal);
+      if (e != cudaSuccess) return cuda_fail(e, "begin capture");
+      for (int k = 0; k < kGraphIters; ++k) {
+        int rc = launch_iteration(s, true, par, str);
+        if (rc) { cudaStreamEndCapture(str, &g); return rc; }
+      }
+      e = cudaStreamEndCapture(str, &g);
+      if (e != cudaSuccess) return cuda_fail(e, "end capture");
+      e = cudaGraphInstantiate(&s->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
+      s->graph_mixed = 1;
+      s->graph_par = par;
+    }
+    while (it < stop && !done) {
+      if (it + kGraphIters > kMaxHist) return set_error(P3D_EINVAL, "iteration history full");
+      e = cudaGraphLaunch(s->graph, str);
+      s->launches += (int64_t)kLaunchesPerIteration * kGraphIters;
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(s->hist_host + kHistCols * it, s->hist + kHistCols * it,
+                            sizeof(double) * kHistCols * kGraphIters, cudaMemcpyDeviceToHost, str);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+      if (e != cudaSuccess) return cuda_fail(e, "mixed graph launch");
+      for (int k = 0; k < kGraphIters; ++k) {
+        s->last_dmax = s->hist_host[kHistCols * (it + k)];
+        if (conv(s->hist_host + kHistCols * (it + k)) && it + k + 1 > 2) {
+          done = true;
+          it += k + 1;
+          break;
+        }
+      }
+      if (!done) it += kGraphIters;
+    }
+  }
+  s->iters_done = it;
+  if (s->ev_stop) cudaEventRecord(s->ev_stop, str);
+  if (iters_out) *iters_out = it;
+  if (dmax_out) *dmax_out = s->last_dmax;
+  return done ? P3D_OK : set_error(P3D_ECONVERGE, "not converged after %lld outer iterations "
+                                   "(largest relative change %.3e)", (long long)it, s->last_dmax);
+}
+
+int p3d_steady_history(p3d_steady_t* h, double* out, int64_t max_n, int64_t* n_out) {
+  if (!h || !out) return set_error(P3D_EINVAL, "null argument");
+  SteadySolver* s = &h->s;
+  int64_t k = s->iters_done < max_n ? s->iters_done : max_n;
+  cudaError_t e = cudaMemcpy(out, s->hist, sizeof(double) * kHistCols * k, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "history copy");
+  if (n_out) *n_out = k;
+  return P3D_OK;
+}
+
+int p3d_steady_get(p3d_steady_t* h, int field, double* host_out) {
+  if (!h || !host_out) return set_error(P3D_EINVAL, "null argument");
+  SteadySolver* s = &h->s;
+  SteadyDev& d = s->d;
+  const double* src = nullptr;
+  cudaStream_t str = s->st->stream;
+  switch (field) {
+    case P3D_F_T_GAS: src = d.t_gas; break;
+    case P3D_F_X_HI: src = d.x_hi; break;
+    case P3D_F_X_H2: src = d.x_h2; break;
+    case P3D_F_X_CP: src = d.x_cp; break;
+    case P3D_F_X_C: src = d.x_c; break;
+    case P3D_F_X_CO: src = d.x_co; break;
+    case P3D_F_X_O: src = d.x_o; break;
+    case P3D_F_X_E: src = d.x_e; break;
+    case P3D_F_G0: src = d.g0; break;
+    case P3D_F_A_V: src = d.av; break;
+    case P3D_F_N_H: src = d.nh_col; break;
+    case P3D_F_T_DUST: src = d.t_dust; break;
+    case P3D_F_GAMMA_PE: src = d.gamma_pe; break;
+    case P3D_F_ZETA: src = d.zeta; break;
+    case P3D_F_F_SH_H2: src = d.fh2; break;
+    case P3D_F_N_H2:
+    case P3D_F_N_CO: {
+      ss_columns_out_kernel<<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(
+          s->n, field == P3D_F_N_H2 ? 1 : 0, s->dens, d.x_h2, d.ds, d.u_h2, d.u_co, s->scratch);
+      src = s->scratch;
+      break;
+    }
+    default: return set_error(P3D_EINVAL, "unknown field %d", field);
+  }
+  cudaError_t e = cudaMemcpyAsync(host_out, src, sizeof(double) * s->n, cudaMemcpyDeviceToHost,
+                                  str);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+  return e == cudaSuccess ? P3D_OK : cuda_fail(e, "steady get");
+}
+
+int p3d_steady_get_ray(p3d_steady_t* h, int32_t* host_out) {
+  if (!h || !host_out) return set_error(P3D_EINVAL, "null argument");
+  SteadySolver* s = &h->s;
+  cudaError_t e = cudaMemcpy(host_out, s->d.ray, sizeof(int32_t) * s->n, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? P3D_OK : cuda_fail(e, "steady get ray");
+}
+
+int p3d_steady_elapsed_ms(p3d_steady_t* h, double* ms) {
+  if (!h || !ms) return set_error(P3D_EINVAL, "null argument");
+  SteadySolver* s = &h->s;
+  if (!s->ev_start) return set_error(P3D_EINVAL, "no reset recorded");
+  cudaError_t e = cudaEventSynchronize(s->ev_stop);
+  float f = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&f, s->ev_start, s->ev_stop);
+  if (e != cudaSuccess) return cuda_fail(e, "elapsed");
+  *ms = f;
+  return P3D_OK;
+}
+
+int p3d_steady_launch_count(p3d_steady_t* h, int64_t* out) {
+  if (!h || !out) return set_error(P3D_EINVAL, "null argument");
+  *out = h->s.launches;
+  return P3D_OK;
+}
+
+int p3d_steady_kernel_times(p3d_steady_t* h, int reps, double* ms4) {
+  if (!h || !ms4 || reps < 1) return set_error(P3D_EINVAL, "bad argument");
+  SteadySolver* s = &h->s;
+  cudaStream_t str = s->st->stream;
+  const SteadyDev& d = s->d;
+  SteadyParams par = s->par;
+  par.count_thr[0] = par.count_thr[1] = par.count_thr[2] = 1.0;
+  par.quiet_tol = 0.0;  // no compaction: every cell solved
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int64_t dims[3] = {s->nx, s->ny, s->nz};
+  unsigned grid = grid_for(s->n, s->st->sms, 4);
+  for (int which = 0; which < 4; ++which) {
+    cudaEventRecord(e0, str);
+    for (int r = 0; r < reps; ++r) {
+      if (which == 0) {
+        for (int axis = 0; axis < 3; ++axis) {
+          int64_t np = s->n / dims[axis];
+          ss_columns_kernel<<<(unsigned)ceil_div(np, 128), 128, 0, str>>>(
+              axis, par.h2_implicit, s->nx, s->ny, s->nz, np, s->dens, d.x_h2, d.x_co, d.fam,
+              d.ds, d.u_h2, d.u_co);
+        }
+      } else if (which == 1) {
+        ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(s->n, d.t_gas, s->parts);
+        ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, s->n, s->glob);
+      } else if (which == 2) {
+        ss_cell_kernel<true><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->glob,
+                                                         s->a_nano, s->a_rest);
+      } else {
+        ss_cell_kernel<false><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->glob,
+                                                          s->a_nano, s->a_rest);
+      }
+    }
+    cudaEventRecord(e1, str);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return cuda_fail(e, "kernel timing");
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    ms4[which] = (double)ms / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return P3D_OK;
+}
+
+int p3d_steady_destroy(p3d_steady_t* h) {
+  delete h;
+  return P3D_OK;
+}
+
+}  // extern "C"

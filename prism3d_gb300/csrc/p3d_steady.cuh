@@ -1,0 +1,60 @@
+// p3d_steady.cuh -- data layout of the steady-state driver.
+#pragma once
+
+#include "p3d_common.cuh"
+#include "p3d_pe.cuh"
+
+namespace p3d {
+
+// Per-cell device arrays (structure of arrays, n cells each, C order of the
+// grid).  Resident for the whole solve.
+struct SteadyDev {
+  // fixed by density (set at reset)
+  const double* dens;
+  double *g0, *av, *nh_col;
+  int32_t* ray;
+  double *ds, *kpd0, *uv0, *kci, *kco0, *hci0, *zeta, *td_rad;
+  int8_t* fam;  // selected ray family: axis * 2 + (1 if cumsum ascends)
+  // state
+  double *t_gas, *x_hi, *x_h2, *x_cp, *x_c, *x_co, *x_o, *x_e;
+  // per-iteration columns
+  double *u_h2, *u_co;
+  // per-cell outer T update memory
+  double *t_prev, *r_prev, *t_lo, *t_hi, *span;
+  // thermal root of the last iteration (warm start of the mixed path)
+  double* t_root;
+  // inputs at the last solve and the change it made (mixed-path compaction)
+  double *u_h2_last, *u_co_last, *b_last, *chg_last;
+  // diagnostics of the last iteration
+  double *fh2, *gamma_pe, *t_dust;
+  int32_t* flags;
+};
+
+struct SteadyParams {
+  double zeta0, x_c_total, x_o_total, x_hcop, t_init, f_nano, e_g;
+  double sigma_nano, sigma_lc, sigma_sil;
+  double w_chem, w_t, chem_rtol, therm_tol;
+  double theta2;  // T_u of CO J = 1 (the ladder spacing 2 h B / k)
+  int chem_max_iter, therm_max_iter, n_rays;
+  int h2_implicit;  // 1: the cell's own H2 half layer is solved implicitly
+  double count_thr[3];  // thresholds of the n_gt counters
+  double quiet_tol;     // mixed path: skip cells quiescent to this level
+  PeGrid pe;
+  LineParams lines;
+};
+
+// Scalars shared between the kernels of one outer iteration.
+struct SteadyGlobals {
+  double t_mean, b_dop;
+  unsigned long long dmax_bits;
+  unsigned long long evals64;  // FP64 net-heating evaluations
+  unsigned int chem_fail, therm_fail;
+  unsigned int n_gt[3];  // cells with relative change > count_thr[k]
+  unsigned int n_active;  // cells solved this iteration
+  int iter;
+};
+
+// Columns of the per-iteration history record.
+constexpr int kHistCols = 9;
+
+}  // namespace p3d

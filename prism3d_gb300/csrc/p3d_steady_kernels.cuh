@@ -1,0 +1,409 @@
+// p3d_steady_kernels.cuh -- kernels of the device-resident steady-state driver.
+//
+// One outer iteration reproduces the physics and ordering of
+// PDRSolver3D.run() (prism3d/solver_3d.py:262-376) on the whole grid:
+//   1. columns: N_H2 and N_CO along each cell's selected FUV ray;
+//   2. grid-mean T for the H2 shielding Doppler width (solver_3d.py:302);
+//   3. one fused per-cell kernel: shielding, PE heating, T_dust, H2
+//      formation, chemistry to steady state (backward-Euler / Newton with the
+//      cell's own H2 column solved implicitly), damping, thermal-balance
+//      root, per-cell T update, convergence measure.
+// G0, A_V, N_H, the cosmic-ray rate and the selected ray depend on density
+// only (fuv_rt_3d.py:284-292: A_V uses N_H), so they are computed once by
+// the full ray march at reset and folded into per-cell constants.
+//
+// Two precisions share the kernels: PLAIN (FP64 everywhere, fixed work per
+// cell, one host synchronisation per iteration) and MIXED (FP32 LU with FP64
+// residual + refinement, FP32 bisection with FP64-certified signs and an
+// FP64 Newton polish of the thermal root, warm starts, iterations captured
+// in a CUDA graph and checked every few launches).
+#pragma once
+
+#include "p3d_common.cuh"
+#include "p3d_newton.cuh"
+#include "p3d_pe.cuh"
+#include "p3d_phys.cuh"
+#include "p3d_rt.cuh"
+#include "p3d_steady.cuh"
+#include "p3d_thermal.cuh"
+#include "p3d_thermal_fast.cuh"
+
+namespace p3d {
+
+// CO ladder and FP32 line tables for this translation unit (filled at
+// p3d_steady_create).
+__constant__ CoLevel c_co_ss[40];
+__constant__ float c_lines32[20];
+__constant__ float c_co32[200];
+
+// ----------------------------------------------------------------- setup
+__global__ void __launch_bounds__(kThreads)
+ss_setup_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restrict__ ray_ds,
+                const int* __restrict__ ray_fam) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double g0 = d.g0[i], av = d.av[i], nh = d.nh_col[i];
+    int r = d.ray[i];
+    bool okr = (r >= 0 && r < p.n_rays);
+    d.ds[i] = okr ? ray_ds[r] : 0.0;
+    d.fam[i] = okr ? (int8_t)ray_fam[r] : (int8_t)-1;
+    double e374 = exp(-3.74 * av);
+    d.kpd0[i] = 4.43e-11 * g0 * e374;
+    d.uv0[i] = g0 * e374;
+    d.kci[i] = 2.56e-10 * g0 * exp(-3.02 * av);
+    d.kco0[i] = 1.71e-10 * g0 * exp(-3.53 * av);
+    d.hci0[i] = 3.0e-10 * g0 * exp(-3.0 * av);
+    d.zeta[i] = cr_rate(nh, p.zeta0);
+    d.td_rad[i] = tdust_rad(g0, av);
+    // analytic initial abundances (solver_3d.py:155-191)
+    double lg = log10(fmax(g0, 0.1));
+    double fh2 = 0.5 * (1.0 + tanh((av - (1.5 + 0.3 * lg)) / 0.8));
+    double xh2 = fmin(fmax(fh2 * 0.5, 1e-6), 0.5);
+    double xhi = fmin(fmax(1.0 - 2.0 * xh2, 1e-6), 1.0);
+    double fco = 0.5 * (1.0 + tanh((av - (3.0 + 0.2 * lg)) / 1.0));
+    double X = p.x_c_total;
+    double xco = fmin(fmax(X * fco * 0.95, 1e-10), X);
+    double xc = fmin(fmax(X * fco * 0.05, 1e-10), X);
+    double xcp = fmin(fmax(X * (1.0 - fco), 1e-10), X);
+    double cs = xcp + xc + xco;
+    double sc = cs > 0.0 ? X / cs : 1.0;
+    xcp *= sc;
+    xc *= sc;
+    xco *= sc;
+    d.x_hi[i] = xhi;
+    d.x_h2[i] = xh2;
+    d.x_cp[i] = xcp;
+    d.x_c[i] = xc;
+    d.x_co[i] = xco;
+    d.x_o[i] = fmax(p.x_o_total - xco, 1e-10);
+    d.x_e[i] = fmax(xcp + p.x_hcop, 1e-10);
+    d.t_gas[i] = p.t_init;
+    d.t_prev[i] = 0.0;
+    d.r_prev[i] = 0.0;
+    d.t_lo[i] = 0.0;
+    d.t_hi[i] = INFINITY;
+    d.span[i] = INFINITY;
+    d.t_root[i] = 0.0;
+    d.u_h2_last[i] = -1.0;
+    d.u_co_last[i] = -1.0;
+    d.b_last[i] = -1.0;
+    d.chg_last[i] = INFINITY;
+    d.flags[i] = 0;
+  }
+}
+
+// --------------------------------------------------------------- columns
+// Thread per pencil of `axis`; both directions.  For cells whose selected
+// ray has this axis and direction: u_h2 = N_H2 and u_co = N_CO, the
+// reference's columns with the cell's own half layer (fuv_rt_3d.py:334-388);
+// with own_implicit the own H2 half layer is left out of u_h2 and added
+// inside the chemistry solve.
+__global__ void __launch_bounds__(128)
+ss_columns_kernel(int axis, int own_implicit, int64_t nx, int64_t ny, int64_t nz,
+                  int64_t n_pencils, const double* __restrict__ dens, const double* __restrict__ xh2,
+                  const double* __restrict__ xco, const int8_t* __restrict__ fam,
+                  const double* __restrict__ ds, double* __restrict__ u_h2,
+                  double* __restrict__ u_co) {
+  int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n_pencils) return;
+  int64_t base, stride, len;
+  if (axis == 0) { base = p; stride = ny * nz; len = nx; }
+  else if (axis == 1) { int64_t i = p / nz, k = p - i * nz; base = i * ny * nz + k; stride = nz; len = ny; }
+  else { base = p * nz; stride = 1; len = nz; }
+  for (int fwd = 1; fwd >= 0; --fwd) {
+    const int8_t want = (int8_t)(axis * 2 + fwd);
+    double s2 = 0.0, s3 = 0.0;
+    for (int64_t t = 0; t < len; ++t) {
+      int64_t c = base + (fwd ? t : (len - 1 - t)) * stride;
+      double n = dens[c];
+      double l2 = n * xh2[c] * 2.0;
+      double l3 = n * xco[c];
+      if (fam[c] == want) {
+        double dsc = ds[c];
+        u_h2[c] = own_implicit ? dsc * s2 : fmax(dsc * (s2 + 0.5 * l2), 0.0);
+        u_co[c] = fmax(dsc * (s3 + 0.5 * l3), 0.0);
+      }
+      s2 += l2;
+      s3 += l3;
+    }
+  }
+}
+
+// ------------------------------------------------------------ reductions
+__global__ void ss_sum_kernel(int64_t n, const double* __restrict__ x, double* __restrict__ part) {
+  __shared__ double sh[kThreads / 32];
+  double s = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    s += x[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w) t += sh[w];
+    part[blockIdx.x] = t;
+  }
+}
+
+__global__ void ss_finalize_kernel(int nparts, const double* __restrict__ part, int64_t n,
+                                   SteadyGlobals* g) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double s = 0.0;
+  for (int b = 0; b < nparts; ++b) s += part[b];
+  double tm = s / (double)n;
+  g->t_mean = tm;
+  g->b_dop = sqrt(2.0 * kKBoltz * tm / (2.0 * kMH)) / 1e5;
+  g->dmax_bits = 0ull;
+  g->evals64 = 0ull;
+  g->chem_fail = 0u;
+  g->therm_fail = 0u;
+  g->n_gt[0] = g->n_gt[1] = g->n_gt[2] = 0u;
+  g->n_active = 0u;
+}
+
+__device__ __forceinline__ void block_max_atomic(double v, unsigned long long* dst) {
+  __shared__ double sh[kThreads / 32];
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, sh[w]);
+    // non-negative doubles order like their bit patterns
+    if (m > 0.0) atomicMax(dst, (unsigned long long)__double_as_longlong(m));
+  }
+}
+
+// ------------------------------------------------- per-cell T update
+// r = G - T_in changes sign at a fixed point of the outer map; each cell
+// keeps the largest T_in with r > 0 (lo) and the smallest with r < 0 (hi).
+// With a bracket: secant step through the last two (T_in, r) pairs, or the
+// geometric midpoint when it leaves the bracket.  Without one: the damped
+// step (1 - w_T) r, limited to `span`, which starts at twice the width of
+// the last lost bracket and grows x4 per step.
+__device__ __forceinline__ double t_update(double t_in, double G, double w_t, double& tp,
+                                           double& rp, double& lo, double& hi, double& span) {
+  double r = G - t_in;
+  double lo_n = r > 0.0 ? fmax(lo, t_in) : lo;
+  double hi_n = r < 0.0 ? fmin(hi, t_in) : hi;
+  bool bad = lo_n >= hi_n;
+  bool had = (lo > 0.0) && isfinite(hi);
+  if (bad && had) span = fmax(2.0 * (hi - lo), 1e-9 * t_in);
+  if (bad) {
+    lo = r > 0.0 ? t_in : 0.0;
+    hi = r < 0.0 ? t_in : INFINITY;
+  } else {
+    lo = lo_n;
+    hi = hi_n;
+  }
+  bool valid = (lo > 0.0) && isfinite(hi);
+  double den = r - rp;
+  double ts = t_in - r * (t_in - tp) / den;
+  bool ok_sec = isfinite(ts) && (den != 0.0) && (tp > 0.0);
+  double mid = sqrt(lo * (valid ? hi : 1.0));
+  bool inside = ok_sec && ts > lo && ts < hi;
+  double step = fmin(fmax((1.0 - w_t) * r, -span), span);
+  if (!valid) span *= 4.0;
+  double tn = valid ? (inside ? ts : mid) : t_in + step;
+  if (r == 0.0) tn = t_in;
+  tp = t_in;
+  rp = r;
+  return tn;
+}
+
+// ----------------------------------------------------------- cell kernel
+template <bool MIXED>
+__global__ void __launch_bounds__(kThreads)
+ss_cell_kernel(int64_t n, SteadyDev d, SteadyParams p, const SteadyGlobals* __restrict__ g_in,
+               SteadyGlobals* g_out, const double* __restrict__ a_nano,
+               const double* __restrict__ a_rest) {
+  const double b_dop = g_in->b_dop;
+  const int iter = g_in->iter;
+  double my_max = 0.0;
+  unsigned int my_gt[3] = {0u, 0u, 0u};
+  unsigned int my_active = 0u;
+  unsigned long long my_evals = 0ull;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double uh2 = d.u_h2[i], uco = d.u_co[i];
+    if (MIXED && iter > 2) {
+      // compaction: a cell whose last solve changed nothing (to quiet_tol)
+      // and whose inputs have not moved since is its own fixed point
+      const double q = p.quiet_tol;
+      if (d.chg_last[i] <= q && fabs(uh2 - d.u_h2_last[i]) <= q * fabs(uh2) &&
+          fabs(uco - d.u_co_last[i]) <= q * fabs(uco) &&
+          fabs(b_dop - d.b_last[i]) <= q * b_dop)
+        continue;
+    }
+    ++my_active;
+    const double nh = d.dens[i];
+    const double tg = d.t_gas[i];
+    const double xe0 = d.x_e[i];
+    double y_old[5] = {d.x_hi[i], d.x_h2[i], d.x_cp[i], d.x_c[i], d.x_co[i]};
+    // dust coupling at the current T (solver_3d.py:509-530)
+    const double gpe = pe_cell(p.pe, a_nano, a_rest, d.g0[i], tg, xe0, nh, p.f_nano, p.e_g);
+    const double td = tdust(d.td_rad[i], nh, tg);
+    const double rh2 = h2_form(tg, td, p.f_nano, p.sigma_nano, p.sigma_lc, p.sigma_sil);
+    const double zeta = d.zeta[i];
+    // chemistry (solver_3d.py:549-557 rates; steady state of chemistry.rs:35-49)
+    ChemCell cc;
+    cc.n_h = nh;
+    cc.kci = d.kci[i];
+    cc.acp = 4.67e-12 * pow(tg / 300.0, -0.6);
+    cc.rh2 = rh2 * nh * 0.5;
+    cc.rcr = 2.5 * zeta * 0.1;
+    cc.xc = p.x_c_total;
+    cc.hcop = p.x_hcop;
+    cc.kpd0 = d.kpd0[i];
+    cc.kco0 = d.kco0[i];
+    cc.kco_cr = 6.0 * zeta;
+    cc.u_h2 = uh2;
+    cc.u_co = uco;
+    cc.ds = p.h2_implicit ? d.ds[i] : 0.0;
+    cc.b_dop = b_dop;
+    chem_prepare(cc);
+    double y[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) y[k] = fmax(y_old[k], 1e-30);
+    double fh2 = 1.0;
+    int citers = 0;
+    int cst = chem_steady_cell<MIXED>(cc, y, p.chem_max_iter, p.chem_rtol, 4.0, &fh2, &citers);
+    const double x_o = fmax(p.x_o_total - y[4], 1e-30);
+    const double x_e = fmax(y[2] + p.x_hcop, 1e-30);
+    double x[5];
+    if (iter > 0 && p.w_chem > 0.0) {
+#pragma unroll
+      for (int k = 0; k < 5; ++k) x[k] = p.w_chem * y_old[k] + (1.0 - p.w_chem) * y[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 5; ++k) x[k] = y[k];
+    }
+    // thermal context (solver_3d.py:693-754)
+    ThermalCtx c;
+    const double uv = d.uv0[i] * fh2;
+    double gf = gpe;
+    gf += 3.3e-11 * uv * x[1] * nh * (0.4 * kEVtoErg);
+    gf += rh2 * x[0] * (nh * nh) * (1.5 * kEVtoErg);
+    gf += 3.0e-10 * uv * x[1] * nh * (2.0 * kEVtoErg) * (nh / (nh + 3e4));
+    gf += zeta * (x[0] + 2.0 * x[1]) * nh * (20.0 * kEVtoErg);
+    gf += d.hci0[i] * x[3] * nh * kEVtoErg;
+    c.gamma_fixed = gf;
+    const double mu = x[1] > 0.5 ? 2.0 : 1.0;
+    c.gg_coeff = 2.0 * 0.35 * 1e-21 * (nh * nh) * sqrt(8.0 * kKBoltz / (kPi * mu * kMH)) * kKBoltz;
+    c.t_dust = td;
+    c.n_e = x_e * nh;
+    c.n_hi = x[0] * nh;
+    c.n_h2 = x[1] * nh;
+    c.n_co = x[4] * nh;
+    c.n_cp_nh = x[2] * nh;
+    c.n_o_nh = x_o * nh;
+    c.n_c_nh = x[3] * nh;
+    int tst = 0, nev = 0;
+    double troot = MIXED ? root_mixed(c, p.lines, c_co_ss, p.theta2, c_lines32, c_co32,
+                                      p.therm_tol, p.therm_max_iter, d.t_root[i], &tst, &nev)
+                         : root_plain(c, p.lines, c_co_ss, p.theta2, p.therm_tol,
+                                      p.therm_max_iter, &tst, &nev);
+    my_evals += (unsigned long long)nev;
+    d.t_root[i] = troot;
+    double tp = d.t_prev[i], rp = d.r_prev[i], lo = d.t_lo[i], hi = d.t_hi[i], sp = d.span[i];
+    double tn = t_update(tg, troot, p.w_t, tp, rp, lo, hi, sp);
+    // convergence measure: largest relative change of T and the species
+    double m = fabs(tn - tg) / tg;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) m = fmax(m, fabs(x[k] - y_old[k]) / fmax(y_old[k], 1e-20));
+    if (!(m == m)) m = INFINITY;
+    my_max = fmax(my_max, m);
+    my_gt[0] += m > p.count_thr[0];
+    my_gt[1] += m > p.count_thr[1];
+    my_gt[2] += m > p.count_thr[2];
+    d.u_h2_last[i] = uh2;
+    d.u_co_last[i] = uco;
+    d.b_last[i] = b_dop;
+    d.chg_last[i] = m;
+    if (cst) atomicAdd(&g_out->chem_fail, 1u);
+    if (tst) atomicAdd(&g_out->therm_fail, 1u);
+    d.x_hi[i] = x[0];
+    d.x_h2[i] = x[1];
+    d.x_cp[i] = x[2];
+    d.x_c[i] = x[3];
+    d.x_co[i] = x[4];
+    d.x_o[i] = x_o;
+    d.x_e[i] = x_e;
+    d.t_gas[i] = tn;
+    d.t_prev[i] = tp;
+    d.r_prev[i] = rp;
+    d.t_lo[i] = lo;
+    d.t_hi[i] = hi;
+    d.span[i] = sp;
+    d.fh2[i] = fh2;
+    d.gamma_pe[i] = gpe;
+    d.t_dust[i] = td;
+  }
+  block_max_atomic(my_max, &g_out->dmax_bits);
+  // counters: warp sums, one atomic per warp
+  for (int o = 16; o > 0; o >>= 1) {
+    my_evals += __shfl_xor_sync(0xffffffffu, my_evals, o);
+    my_active += __shfl_xor_sync(0xffffffffu, my_active, o);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) my_gt[k] += __shfl_xor_sync(0xffffffffu, my_gt[k], o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&g_out->evals64, my_evals);
+    if (my_active) atomicAdd(&g_out->n_active, my_active);
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      if (my_gt[k]) atomicAdd(&g_out->n_gt[k], my_gt[k]);
+  }
+}
+
+// N_H2 (which = 1) or N_CO (which = 0) of the selected ray for output:
+// N_H2 adds the cell's own half layer to the upstream sum.
+__global__ void ss_columns_out_kernel(int64_t n, int which, const double* __restrict__ dens,
+                                      const double* __restrict__ xh2,
+                                      const double* __restrict__ ds,
+                                      const double* __restrict__ u_h2,
+                                      const double* __restrict__ u_co, double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = which ? u_h2[i] + ds[i] * dens[i] * xh2[i] : u_co[i];
+}
+
+// hist[kHistCols it ...] = (largest relative change, chemistry failures,
+// thermal failures, cells changing more than count_thr[0..2], FP64
+// net-heating evaluations, mean T, cells solved) of iteration `it`; then
+// advance the counter.
+__global__ void ss_record_kernel(SteadyGlobals* g, double* hist, int max_hist) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    int it = g->iter;
+    if (it >= 0 && it < max_hist) {
+      double* h = hist + (int64_t)kHistCols * it;
+      h[0] = __longlong_as_double((long long)g->dmax_bits);
+      h[1] = (double)g->chem_fail;
+      h[2] = (double)g->therm_fail;
+      h[3] = (double)g->n_gt[0];
+      h[4] = (double)g->n_gt[1];
+      h[5] = (double)g->n_gt[2];
+      h[6] = (double)g->evals64;
+      h[7] = g->t_mean;
+      h[8] = (double)g->n_active;
+    }
+    g->iter = it + 1;
+  }
+}
+
+__global__ void ss_reset_globals_kernel(SteadyGlobals* g) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    g->t_mean = 0.0;
+    g->b_dop = 0.0;
+    g->dmax_bits = 0ull;
+    g->evals64 = 0ull;
+    g->chem_fail = 0u;
+    g->therm_fail = 0u;
+    g->n_gt[0] = g->n_gt[1] = g->n_gt[2] = 0u;
+    g->n_active = 0u;
+    g->iter = 0;
+  }
+}
+
+}  // namespace p3d

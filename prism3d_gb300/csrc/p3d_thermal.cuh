@@ -121,3 +121,48 @@ cudaError_t launch_thermal13(int64_t n, const double* const* ctx, const LinePara
                              cudaStream_t s);
 
 }  // namespace p3d
+
+namespace p3d {
+
+// Bisection of [10, 1e5] K (rust/src/thermal.rs:231-243) followed by a
+// safeguarded Newton iteration (Newton with a forward-difference slope,
+// bisection whenever the step leaves the bracket or does not halve the
+// previous step) until |dT| <= tol T or the bracket is narrower than tol T.
+// A sign change at one of the discontinuities of the net heating (the CO
+// ladder break, T = 100 K, T = 3000 K) converges to the jump.
+// Returns the root; *status 0 converged, 1 iteration limit.
+__device__ __forceinline__ double thermal_root64(const ThermalCtx& c, const LineParams& lp,
+                                                 const CoLevel* __restrict__ co, int n_bisect,
+                                                 int max_newton, double tol, int* status,
+                                                 int* iters) {
+  double t_lo = 10.0, t_hi = 1e5;
+  for (int k = 0; k < n_bisect; ++k) {
+    double t_mid = sqrt(t_lo * t_hi);
+    if (net_heating64(t_mid, c, lp, co) > 0.0) t_lo = t_mid; else t_hi = t_mid;
+  }
+  double t = sqrt(t_lo * t_hi);
+  double dx_old = t_hi - t_lo, dx = dx_old;
+  *status = 1;
+  int k;
+  for (k = 0; k < max_newton; ++k) {
+    double f = net_heating64(t, c, lp, co);
+    double eps = t * 1e-7;
+    double df = (net_heating64(t + eps, c, lp, co) - f) / eps;
+    if (f > 0.0) t_lo = t; else t_hi = t;
+    if (f == 0.0) { *status = 0; ++k; break; }
+    double tn = t - f / df;
+    if (!(df != 0.0) || !(tn > t_lo && tn < t_hi) || fabs(2.0 * f) > fabs(dx_old * df)) {
+      dx_old = dx;
+      tn = 0.5 * (t_lo + t_hi);
+    } else {
+      dx_old = dx;
+    }
+    dx = tn - t;
+    t = tn;
+    if (fabs(dx) <= tol * t || t_hi - t_lo <= tol * t) { *status = 0; ++k; break; }
+  }
+  *iters = k;
+  return t;
+}
+
+}  // namespace p3d

@@ -1,0 +1,163 @@
+"""GPU steady-state solver with the constructor and state of the reference's
+PDRSolver3D (prism3d/solver_3d.py:34-149).
+
+    s = PDRSolverGPU(density, box_size, G0_external=directional_G0(...),
+                     zeta_CR_0=2e-16, nside_rt=2, T_init=100.0)
+    converged = s.run(convergence_tol=1e-10, mixed=True)
+    s.T_gas, s.x_H2, ...          # (nx, ny, nz) NumPy arrays
+    s.save("state.npz")            # the reference's save() keys
+
+The whole outer iteration runs on the device (libprism3d_gb300.so,
+p3d_steady_*): the FUV ray march once (G0, A_V, N_H and the selected ray
+depend on density only), then per iteration the selected-ray H2/CO columns,
+shielding, cosmic rays, dust coupling, steady-state chemistry and the
+thermal root.  ``mixed=False`` is the plain FP64 path, ``mixed=True`` the
+batched mixed-precision path.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+from . import constants as C
+from .core import directional_G0, healpix_directions  # noqa: F401
+from .tables import DustTables, line_params
+
+FIELDS = {"T_gas": 0, "x_HI": 1, "x_H2": 2, "x_Cp": 3, "x_C": 4, "x_CO": 5, "x_O": 6, "x_e": 7,
+          "G0": 8, "A_V": 9, "N_H": 10, "N_H2": 11, "N_CO": 12, "T_dust": 13, "Gamma_PE": 14,
+          "zeta_CR": 15, "f_sh_H2": 16}
+
+
+class NotConvergedError(RuntimeError):
+    pass
+
+
+class PDRSolverGPU:
+    """Device-resident PRISM-3D steady state on one GB300."""
+
+    def __init__(self, density, box_size, G0_external=1.0, zeta_CR_0=2e-16, nside_rt=1,
+                 T_init=50.0, tables=None):
+        self.density = np.ascontiguousarray(density, dtype=np.float64)
+        if self.density.ndim != 3:
+            raise ValueError("density must be (nx, ny, nz)")
+        self.nx, self.ny, self.nz = self.density.shape
+        self.n_cells = self.density.size
+        self.box_size = float(box_size)
+        self.cell_size = self.box_size / self.nx
+        self.G0_external = G0_external
+        self.zeta_CR_0 = float(zeta_CR_0)
+        self.nside_rt = int(nside_rt)
+        self.T_init = float(T_init)
+        self.tables = tables if tables is not None else DustTables()
+        self.history = []
+        self.iterations = 0
+        self._h = ctypes.c_void_p()
+        tb = self.tables
+        dirs, w = healpix_directions(self.nside_rt)
+        g = np.atleast_1d(np.asarray(G0_external, dtype=np.float64)).ravel()
+        sig = np.array([tb.sigma_nano, tb.sigma_largeC, tb.sigma_Sil])
+        lines = line_params()
+        self._keep = (dirs, w, g, sig, lines)
+        p = L.dptr
+        L.call("p3d_steady_create", ctypes.byref(self._h), self.nx, self.ny, self.nz,
+               p(self.density), p(g), g.size, self.cell_size, p(dirs), p(w), len(dirs),
+               self.zeta_CR_0, C.x_C_total, C.x_O_total, self.T_init,
+               p(np.ascontiguousarray(tb.pe_table)), tb.n_bins, tb.log_psi_min,
+               tb.log_psi_step, tb.n_psi, tb.eg_min, tb.eg_step, tb.n_Eg,
+               p(tb.bin_sigma_abs), p(tb.bin_dn_da_da), p(tb.bin_is_nano.astype(np.float64)),
+               p(sig), *[p(a) for a in lines])
+        self.reset()
+
+    def reset(self):
+        """Ray march, per-cell constants and analytic initial abundances."""
+        L.call("p3d_steady_reset", self._h)
+        self.iterations = 0
+
+    def run(self, max_iterations=2000, convergence_tol=1e-8, mixed=True, w_chem=0.5, w_T=0.5,
+            n_allow=None, raise_on_failure=False):
+        """Outer iterations until at most n_allow cells (default
+        max(8, 1e-5 n_cells)) change by more than convergence_tol (relative,
+        T_gas and species above 1e-20).  Returns True when converged."""
+        if n_allow is None:
+            n_allow = max(8, int(1e-5 * self.n_cells))
+        it = L._i64(0)
+        dm = L._f64(0.0)
+        rc = L.lib.p3d_steady_run(self._h, int(bool(mixed)), int(max_iterations),
+                                  float(convergence_tol), int(n_allow), float(w_chem), float(w_T),
+                                  ctypes.byref(it), ctypes.byref(dm))
+        self.iterations = int(it.value)
+        self.last_change = float(dm.value)
+        if rc == -5:
+            if raise_on_failure:
+                raise NotConvergedError(L.lib.p3d_last_error().decode())
+            return False
+        L.check("p3d_steady_run", rc)
+        return True
+
+    def get(self, name):
+        out = np.empty(self.n_cells)
+        L.call("p3d_steady_get", self._h, FIELDS[name], L.dptr(out))
+        return out.reshape(self.density.shape)
+
+    def elapsed_ms(self):
+        """Device time of the last reset + run (CUDA events, library stream)."""
+        ms = L._f64(0.0)
+        L.call("p3d_steady_elapsed_ms", self._h, ctypes.byref(ms))
+        return float(ms.value)
+
+    def launch_count(self):
+        """Kernels launched on the device since the last reset."""
+        c = L._i64(0)
+        L.call("p3d_steady_launch_count", self._h, ctypes.byref(c))
+        return int(c.value)
+
+    def selected_ray(self):
+        out = np.empty(self.n_cells, dtype=np.int32)
+        L.call("p3d_steady_get_ray", self._h, L.iptr(out))
+        return out.reshape(self.density.shape)
+
+    HISTORY_COLUMNS = ("max_rel_change", "chem_fail", "therm_fail", "n_gt_100tol", "n_gt_tol",
+                       "n_gt_tol/100", "fp64_net_heating_evals", "t_mean", "n_active")
+
+    def convergence_history(self):
+        """(iterations, 9) array, columns HISTORY_COLUMNS."""
+        h = np.empty((max(self.iterations, 1), len(self.HISTORY_COLUMNS)))
+        n = L._i64(0)
+        L.call("p3d_steady_history", self._h, L.dptr(h), h.shape[0], ctypes.byref(n))
+        return h[: n.value]
+
+    def __getattr__(self, name):
+        if name in FIELDS:
+            return self.get(name)
+        raise AttributeError(name)
+
+    def state(self):
+        return {k: self.get(k) for k in FIELDS}
+
+    def save(self, filepath):
+        """np.savez_compressed with the keys of PDRSolver3D.save()
+        (solver_3d.py:1150-1170), so the reference's load() reads it."""
+        st = self.state()
+        shp = self.density.shape
+        np.savez_compressed(
+            filepath, density=self.density, T_gas=st["T_gas"], T_dust=st["T_dust"],
+            G0=st["G0"], A_V=st["A_V"], N_H=st["N_H"], N_H2=st["N_H2"], N_CO=st["N_CO"],
+            zeta_CR=st["zeta_CR"], x_HI=st["x_HI"], x_H2=st["x_H2"], x_Cp=st["x_Cp"],
+            x_C=st["x_C"], x_CO=st["x_CO"], x_O=st["x_O"], x_e=st["x_e"],
+            x_OH=1e-9 + 9e-8 * np.clip(10.0 * st["x_H2"], 0, 1), x_H2O=np.full(shp, 1e-8),
+            x_HCOp=np.full(shp, 1e-10), Gamma_PE=st["Gamma_PE"], f_nano=np.ones(shp),
+            E_g=np.full(shp, 0.1), box_size=self.box_size,
+            G0_external=np.max(np.atleast_1d(self.G0_external)), zeta_CR_0=self.zeta_CR_0)
+
+    def close(self):
+        if self._h:
+            L.lib.p3d_steady_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -691,3 +691,54 @@ def _from_zvars(st, z):
     st["x_Cp"] = X_C / (1.0 + r1 + r2)
     st["x_CO"] = r1 * st["x_Cp"]
     st["x_C"] = r2 * st["x_Cp"]
+
+
+def map_residual(st_in, density, G0_external, cell_size, nside, zeta0, tables=None, lines=None):
+    """Apply the steady-state outer map once (without damping or T update)
+    to a state and return (x_star, G, ray): the chemistry steady state and
+    the thermal root for that state's columns, grid-mean T and T.  At a fixed
+    point x_star equals the state's abundances and G its T (or T sits on a
+    sign change of G - T at a discontinuity of the thermal balance)."""
+    if tables is None:
+        from prism3d_gb300.tables import DustTables
+        tables = DustTables()
+    if lines is None:
+        from prism3d_gb300.tables import line_params
+        lines = line_params()
+    dirs, _ = healpix_directions(nside)
+    st = init_state(density, G0_external, zeta0, 100.0)
+    for k, v in st_in.items():
+        st[k] = np.array(v, dtype=np.float64, copy=True)
+    n = st["density"]
+    G0, AV, NH, _, _, ray = fuv_field_3d(n, G0_external, cell_size, None, None, nside,
+                                         return_ray=True)
+    st["G0"], st["A_V"], st["N_H"] = G0, AV, NH
+    const = steady_constants(st, zeta0)
+    st["zeta_CR"] = const["zeta"]
+    ds = ray_ds(dirs, cell_size)[ray]
+    NH2, NCO = selected_columns(n, st["x_H2"], st["x_CO"], ray, dirs, cell_size)
+    b_dop = np.sqrt(2.0 * k_boltz * np.mean(st["T_gas"]) / m_H2) / 1e5
+    update_dust(st, tables)
+    a_cp = 4.67e-12 * np.power(st["T_gas"] / 300.0, -0.6)
+    sp = ("x_HI", "x_H2", "x_Cp", "x_C", "x_CO", "x_O", "x_e")
+    xs = [np.ascontiguousarray(st[k], dtype=np.float64).ravel().copy() for k in sp]
+    _, _, status, fsh = chem_steady(
+        n, const["kpd0"], const["kci"], a_cp, const["kco0"], st["R_H2"] * n * 0.5,
+        2.5 * const["zeta"] * 0.1, X_C, *xs, st["x_HCOp"], rtol=1e-12,
+        selfshield=(6.0 * const["zeta"], NH2, NCO, ds, b_dop))
+    shp = n.shape
+    x_star = {k: a.reshape(shp) for k, a in zip(sp, xs)}
+    st2 = dict(st)
+    st2.update(x_star)
+    for k in ("x_HI", "x_H2", "x_Cp", "x_C", "x_CO"):
+        st2[k] = st[k]  # at a fixed point the damped state equals the input
+    ctx = thermal_ctx(st2, fsh[0].reshape(shp))
+    G, _, _ = thermal_root(ctx, *lines, tol=1e-12)
+    return x_star, G.reshape(shp), ray, ctx
+
+
+def net_heating_at(ctx, t, lines=None):
+    if lines is None:
+        from prism3d_gb300.tables import line_params
+        lines = line_params()
+    return net_heating(ctx, np.ascontiguousarray(t).ravel(), *lines)

@@ -133,6 +133,29 @@ int p3d_pe_heating_vec_dev(const double *pe_table, int64_t n_bins, double log_ps
                            const double *e_g, double *gamma_pe_out, void *stream);
 
 /* ---------------------------------------------------------------------
+ * Photoelectric heating that allocates no device memory.  No counterpart
+ * in the reference: for callers that cannot let a library allocate (work
+ * recorded inside a CUDA stream capture, embedders that fix the device
+ * memory budget up front or own every device byte).  Same arguments and
+ * result as p3d_pe_heating_vec_dev (device pointers for pe_table and the
+ * per-cell arrays, host pointers for the bin vectors, stream NULL = default
+ * stream), but its scratch is a fixed device array of 2 x 8192 + 3 x 256
+ * doubles (137 KB, held by every device that loads the library until the
+ * process exits): n_psi * n_eg <= 8192 and n_bins <= 256, larger tables are
+ * rejected with P3D_EINVAL.  The first call on a device looks up the
+ * array's device address with that device current; make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race; serialise them (one stream, or events).
+ * ------------------------------------------------------------------- */
+int p3d_pe_heating_vec_noalloc(const double *pe_table, int64_t n_bins, double log_psi_min,
+                               double log_psi_step, int64_t n_psi, double eg_min,
+                               double eg_step, int64_t n_eg, const double *bin_sigma_abs,
+                               const double *bin_dn_da_da, const double *bin_is_nano,
+                               int64_t n_cells, const double *g0, const double *t_gas,
+                               const double *x_e, const double *n_h, const double *f_nano,
+                               const double *e_g, double *gamma_pe_out, void *stream);
+
+/* ---------------------------------------------------------------------
  * Ray set of the reference (prism3d/radiative_transfer/fuv_rt.py:19-57):
  * 12*nside^2 Fibonacci-spiral unit vectors dirs [n_rays][3] and equal
  * weights 4 pi / n_rays.  Computed with the C math library; Python callers

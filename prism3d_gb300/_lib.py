@@ -34,6 +34,8 @@ SIGNATURES = {
                           [_D] * 7,
     "p3d_pe_heating_vec_dev": [_D, _i64, _f64, _f64, _i64, _f64, _f64, _i64, _D, _D, _D, _i64] +
                               [_D] * 7 + [_vp],
+    "p3d_pe_heating_vec_noalloc": [_D, _i64, _f64, _f64, _i64, _f64, _f64, _i64, _D, _D, _D,
+                                   _i64] + [_D] * 7 + [_vp],
     "p3d_healpix_directions": [_i64, _D, _D],
     "p3d_fuv_field_3d": [_i64, _i64, _i64, _D, _D, _D, _D, _i64, _f64, _D, _D, _i64] + [_D] * 5 +
                         [_I32],

@@ -552,8 +552,10 @@ def t_update(T_in, G, mem, w_T=0.5):
     at the width of the last lost bracket and grows x4 per step, so a cell
     whose fixed point drifts searches locally instead of jumping.  Cells
     whose fixed point sits on a discontinuity of G (the thermal root jumps
-    between branches) converge to the jump instead of oscillating.
-    mem = (T_prev, r_prev, lo, hi, span) per cell."""
+    between branches) converge to the jump instead of oscillating; once the
+    bracket is narrower than 4e-12 T the cell hops across it every iteration,
+    so the jump is re-verified and a bracket made stale by the rest of the
+    grid breaks.  mem = (T_prev, r_prev, lo, hi, span) per cell."""
     r = G - T_in
     Tp, rp, lo, hi, span = mem
     lo_n = np.where(r > 0, np.maximum(lo, T_in), lo)
@@ -573,6 +575,10 @@ def t_update(T_in, G, mem, w_T=0.5):
     step = np.clip((1.0 - w_T) * r, -span, span)
     span = np.where(valid, span, span * 4.0)
     Tn = np.where(valid, np.where(inside, ts, mid), T_in + step)
+    # collapsed bracket: hop just across it, so the next residual re-checks
+    # the jump (a bracket left over from an earlier map then breaks)
+    tiny = valid & (hi - lo <= 4e-12 * T_in)
+    Tn = np.where(tiny, np.where(T_in <= lo, hi * (1 + 1e-12), lo * (1 - 1e-12)), Tn)
     Tn = np.where(r == 0, T_in, Tn)
     return Tn, (T_in.copy(), r, lo, hi, span)
 
@@ -659,6 +665,7 @@ def steady_run(density, G0_external, cell_size, nside=1, zeta0=2e-16, T_init=100
         f_h2 = fsh[0].reshape(shp)
         ctx = thermal_ctx(st, f_h2)
         t, titers, tstatus = thermal_root(ctx, *lines, tol=therm_tol)
+        st["T_root"] = t.reshape(shp)
         st["T_gas"], mem = t_update(old["T_gas"], t.reshape(shp), mem, w_T)
         d = {"T": float(np.max(np.abs(st["T_gas"] - old["T_gas"]) / old["T_gas"]))}
         for k in species:

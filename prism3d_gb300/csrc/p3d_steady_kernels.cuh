@@ -181,7 +181,9 @@ __device__ __forceinline__ void block_max_atomic(double v, unsigned long long* d
 // With a bracket: secant step through the last two (T_in, r) pairs, or the
 // geometric midpoint when it leaves the bracket.  Without one: the damped
 // step (1 - w_T) r, limited to `span`, which starts at twice the width of
-// the last lost bracket and grows x4 per step.
+// the last lost bracket and grows x4 per step.  A bracket narrower than
+// 4e-12 T makes the cell hop across it each iteration: a genuine jump keeps
+// it, a bracket made stale by the rest of the grid breaks.
 __device__ __forceinline__ double t_update(double t_in, double G, double w_t, double& tp,
                                            double& rp, double& lo, double& hi, double& span) {
   double r = G - t_in;
@@ -206,6 +208,9 @@ __device__ __forceinline__ double t_update(double t_in, double G, double w_t, do
   double step = fmin(fmax((1.0 - w_t) * r, -span), span);
   if (!valid) span *= 4.0;
   double tn = valid ? (inside ? ts : mid) : t_in + step;
+  // collapsed bracket: hop just across it, so the next residual re-checks
+  // the jump (a bracket left over from an earlier map then breaks)
+  if (valid && hi - lo <= 4e-12 * t_in) tn = (t_in <= lo) ? hi * (1.0 + 1e-12) : lo * (1.0 - 1e-12);
   if (r == 0.0) tn = t_in;
   tp = t_in;
   rp = r;

@@ -128,7 +128,8 @@ def run_gb300(args, ws, rank, local):
 
     def solve(mixed=True, max_it=4000):
         s.reset()
-        return s.run(max_iterations=max_it, convergence_tol=args.tol, mixed=mixed, n_allow=n_allow)
+        return s.run(max_iterations=max_it, convergence_tol=args.tol, mixed=mixed, n_allow=n_allow,
+                     w_chem=args.w_chem)
 
     for _ in range(args.warmup):
         solve()
@@ -157,7 +158,8 @@ def run_gb300(args, ws, rank, local):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     s2 = PDRSolverGPU(dens, box, G0_external=g0, zeta_CR_0=zeta, nside_rt=nside, T_init=100.0)
-    s2.run(max_iterations=4000, convergence_tol=args.tol, mixed=True, n_allow=n_allow)
+    s2.run(max_iterations=4000, convergence_tol=args.tol, mixed=True, n_allow=n_allow,
+           w_chem=args.w_chem)
     outs = [s2.get(k) for k in ("T_gas", "x_HI", "x_H2", "x_Cp", "x_C", "x_CO", "x_O", "x_e")]
     t_e2e = time.perf_counter() - t0
     s2.close()
@@ -167,14 +169,15 @@ def run_gb300(args, ws, rank, local):
     s.reset()
     if args.plain_full:
         t0 = time.perf_counter()
-        okp = s.run(max_iterations=4000, convergence_tol=args.tol, mixed=False, n_allow=n_allow)
+        okp = s.run(max_iterations=4000, convergence_tol=args.tol, mixed=False, n_allow=n_allow,
+                    w_chem=args.w_chem)
         tp = time.perf_counter() - t0
         plain = {"value": n / tp, "unit": "cells/s", "iterations": s.iterations,
                  "converged": bool(okp), "seconds": tp, "sample": "full solve"}
     else:
         k = args.plain_iters
         t0 = time.perf_counter()
-        s.run(max_iterations=k, convergence_tol=1e-300, mixed=False, n_allow=0)
+        s.run(max_iterations=k, convergence_tol=1e-300, mixed=False, n_allow=0, w_chem=args.w_chem)
         tp = time.perf_counter() - t0
         ms_it = 1e3 * tp / k
         est = n / (ms_it * 1e-3 * float(np.mean(iters)))
@@ -182,11 +185,16 @@ def run_gb300(args, ws, rank, local):
                  "value_est": est, "unit": "cells/s",
                  "note": "estimate = n_cells / (ms_per_iter x the mixed solve's iteration "
                          "count); --plain-full measures the full plain solve"}
-    # dominant-kernel roofline: the selected-ray column pass (HBM-bound), timed live
-    kt = kernel_times(s)
+    # rooflines, timed live from the 14th outer iteration of a fresh solve (the
+    # state the per-cell FP64 count was measured on), every cell solved
+    s.reset()
+    s.run(max_iterations=13, convergence_tol=1e-300, mixed=True, n_allow=0, w_chem=args.w_chem)
+    kt = kernel_times(s, reps=1)
     hbm, peak_kind = measured_peaks()
+    fp64_peak = fp64_peak_tflops()
     col_bytes = 49.0 * n  # read n_H, x_H2, x_CO, ds, family once; write N_H2, N_CO
-    achieved = col_bytes / (kt["columns_ms"] * 1e-3) / 1e9
+    col_gbs = col_bytes / (kt["columns_ms"] * 1e-3) / 1e9
+    cell_tf = FP64_OPS_PER_CELL_SOLVE * n / (kt["cell_mixed_ms"] * 1e-3) / 1e12
     out = {
         "metric": METRIC, "value": value, "unit": "cells/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True,
@@ -194,7 +202,7 @@ def run_gb300(args, ws, rank, local):
         "data": "synthetic (seeded Orion-Bar-like slab, prism3d_gb300/fields.py)",
         "config": {"workload": f"{args.workload}: 128^3 tanh-ramp slab 1e3->1e5 x lognormal "
                                "0.8, G0=2.6e4 on -x, 48 rays, zeta=2e-16, 0.005 pc cells",
-                   "n_cells": n, "tol": args.tol, "n_allow": n_allow,
+                   "n_cells": n, "tol": args.tol, "n_allow": n_allow, "w_chem": args.w_chem,
                    "outer_iterations": iters, "converged": oks,
                    "l2": "per-step state 0.6 GB > 126 MB L2 (no flush)",
                    "parallelism": f"replicas x{ws}"},
@@ -202,11 +210,17 @@ def run_gb300(args, ws, rank, local):
                 "d2h_bytes_per_step": int(d2h)},
         "plain_fp64": plain,
         "mixed_vs_plain": (value / ws) / plain.get("value", plain.get("value_est")),
-        "roofline": {"kernel": "ss_columns_kernel (3 axis passes, one outer iteration)",
-                     "bound": "hbm", "achieved": achieved, "peak": hbm,
-                     "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
-                     "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": col_bytes},
+        "roofline": {"kernel": "ss_cell_kernel<mixed> (98% of solve time), every cell solved",
+                     "bound": "fp64", "achieved": cell_tf, "peak": fp64_peak,
+                     "unit": "TFLOP/s", "frac": cell_tf / fp64_peak, "traffic": None,
+                     "peak_source": "measured live: DFMA-chain kernel on this GPU",
+                     "algorithmic_flops_per_launch": FP64_OPS_PER_CELL_SOLVE * n,
+                     "per_unit": f"{FP64_OPS_PER_CELL_SOLVE:.0f} FP64 flops per cell solve "
+                                 "(ncu instruction counts, profiles/cell_kernel_slab96.md)"},
+        "roofline_hbm": {"kernel": "ss_columns_kernel (3 axis passes, one outer iteration)",
+                         "bound": "hbm", "achieved": col_gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": col_gbs / hbm, "traffic": None, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": col_bytes},
         "kernel_times_ms": kt,
         "fp64_net_heating_evals_per_cell_iter": float(np.mean(hist[:, 6]) / n),
         "gpu_launches": int(sum(launches)),
@@ -214,6 +228,21 @@ def run_gb300(args, ws, rank, local):
     }
     out["cpu_baseline"] = cpu_baseline(args, dens, g0, nside, zeta, cell, float(np.mean(iters)))
     return out
+
+
+# FP64 flops (DFMA = 2, DADD/DMUL = 1) per cell solve of the mixed cell
+# kernel on the 14th outer iteration of the 96^3 slab, every cell active, from
+# the ncu instruction counts in profiles/cell_kernel_slab96.md.
+FP64_OPS_PER_CELL_SOLVE = 5330.0
+
+
+def fp64_peak_tflops():
+    import ctypes
+
+    from prism3d_gb300 import _lib as L
+    v = ctypes.c_double(0.0)
+    L.call("p3d_fp64_peak_tflops", ctypes.byref(v))
+    return float(v.value)
 
 
 def kernel_times(s, reps=10):
@@ -283,6 +312,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="slab128")
     ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--w-chem", type=float, default=0.1,
+                    help="abundance damping (the reference uses 0.5)")
     ap.add_argument("--plain-full", action="store_true")
     ap.add_argument("--plain-iters", type=int, default=20)
     ap.add_argument("--ref-iters", type=int, default=700)

@@ -263,6 +263,10 @@ int p3d_steady_destroy(p3d_steady_t *s);
 /* Device time (CUDA events on the library stream) from the start of the
  * last p3d_steady_reset to the end of the last p3d_steady_run. */
 int p3d_steady_elapsed_ms(p3d_steady_t *s, double *ms);
+/* Measured FP64 FMA throughput of the current device in TFLOP/s (a DFMA
+ * chain kernel timed with CUDA events): the peak the per-cell kernels, which
+ * are bound by the FP64 pipe, are reported against. */
+int p3d_fp64_peak_tflops(double *tflops);
 /* Kernels launched on the device since the last p3d_steady_reset. */
 int p3d_steady_launch_count(p3d_steady_t *s, int64_t *out);
 /* Mean time (ms) over reps launches on the current state of: the three

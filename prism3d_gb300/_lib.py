@@ -52,6 +52,7 @@ SIGNATURES = {
     "p3d_steady_destroy": [_vp],
     "p3d_steady_launch_count": [_vp, _I64],
     "p3d_steady_elapsed_ms": [_vp, _D],
+    "p3d_fp64_peak_tflops": [_D],
     "p3d_steady_kernel_times": [_vp, ctypes.c_int, _D],
 }
 _RESTYPES = {"p3d_version": ctypes.c_char_p, "p3d_last_error": ctypes.c_char_p}

@@ -23,7 +23,7 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libprism3d_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-ftz=false", "-prec-div=true", "-prec-sqrt=true",
-              "-Xcompiler", "-Wall"]
+              "-Xcompiler", "-Wall"] + os.environ.get("P3D_NVCC_EXTRA", "").split()
 
 
 def nvcc():

@@ -155,8 +155,11 @@ __device__ __forceinline__ void lu5_solve(const R (*LU)[5], const int* perm, con
   for (int r = 0; r < 5; ++r) x[r] = (double)y[r];
 }
 
-// Solve A d = b (A, b row-equilibrated in FP64).  MIXED: factor in FP32,
-// refine twice with FP64 residuals.
+// Solve A d = b (A, b row-equilibrated).  MIXED: factor and solve in FP32;
+// the Newton iteration around it evaluates the nonlinear residual f in FP64,
+// so each iteration refines the previous one's FP32 solve (the iteration
+// converges to the FP64 root; the contraction per step is the FP32 solve's
+// relative error, ~1e-6).
 template <bool MIXED>
 __device__ __forceinline__ bool solve5(const double (*A)[5], const double* b, double* d) {
   if (!MIXED) {
@@ -178,20 +181,6 @@ __device__ __forceinline__ bool solve5(const double (*A)[5], const double* b, do
       for (int c = 0; c < 5; ++c) LU[r][c] = (float)A[r][c];
     if (!lu5<float>(LU, perm)) return false;
     lu5_solve<float>(LU, perm, b, d);
-#pragma unroll
-    for (int pass = 0; pass < 2; ++pass) {
-      double res[5], corr[5];
-#pragma unroll
-      for (int r = 0; r < 5; ++r) {
-        double s = b[r];
-#pragma unroll
-        for (int c = 0; c < 5; ++c) s -= A[r][c] * d[c];
-        res[r] = s;
-      }
-      lu5_solve<float>(LU, perm, res, corr);
-#pragma unroll
-      for (int r = 0; r < 5; ++r) d[r] += corr[r];
-    }
     return true;
   }
 }
@@ -211,33 +200,61 @@ __device__ __forceinline__ int chem_steady_cell(const ChemCell& p, double* y, in
   int it;
   int status = 1;
   for (it = 0; it < max_iter; ++it) {
-    double f[5], J[5][5], A[5][5], d[5], b[5], sc[5], yn[5];
+    double f[5], J[5][5], d[5], sc[5], yn[5];
     chem5_eval(p, y, f, J, sc, fh2);
+    bool ok;
+    if (MIXED) {
+      // FP32 system: columns scaled by y, rows equilibrated, FP64 residual
+      float A[5][5], b[5];
+      int perm[5];
 #pragma unroll
-    for (int r = 0; r < 5; ++r) {
-      int os = ode_species(r);
-      double m = 0.0;
-      if (os >= 0) {
+      for (int r = 0; r < 5; ++r) {
+        int os = ode_species(r);
+        float m = 0.0f;
 #pragma unroll
-        for (int c = 0; c < 5; ++c) A[r][c] = -J[r][c];
-        A[r][os] += inv_dt;
-        b[r] = f[r];
-      } else {
+        for (int c = 0; c < 5; ++c) {
+          double a = (os >= 0) ? -J[r][c] + (c == os ? inv_dt : 0.0) : J[r][c];
+          A[r][c] = (float)(a * y[c]);
+          m = fmaxf(m, fabsf(A[r][c]));
+        }
+        float inv = 1.0f / m;
 #pragma unroll
-        for (int c = 0; c < 5; ++c) A[r][c] = J[r][c];
-        b[r] = -f[r];
+        for (int c = 0; c < 5; ++c) A[r][c] *= inv;
+        b[r] = (float)((os >= 0 ? f[r] : -f[r]) / (double)m);
       }
+      double bd[5];
 #pragma unroll
-      for (int c = 0; c < 5; ++c) {
-        A[r][c] *= y[c];
-        m = fmax(m, fabs(A[r][c]));
+      for (int r = 0; r < 5; ++r) bd[r] = b[r];
+      ok = lu5<float>(A, perm);
+      if (ok) lu5_solve<float>(A, perm, bd, d);
+    } else {
+      double A[5][5], b[5];
+#pragma unroll
+      for (int r = 0; r < 5; ++r) {
+        int os = ode_species(r);
+        double m = 0.0;
+        if (os >= 0) {
+#pragma unroll
+          for (int c = 0; c < 5; ++c) A[r][c] = -J[r][c];
+          A[r][os] += inv_dt;
+          b[r] = f[r];
+        } else {
+#pragma unroll
+          for (int c = 0; c < 5; ++c) A[r][c] = J[r][c];
+          b[r] = -f[r];
+        }
+#pragma unroll
+        for (int c = 0; c < 5; ++c) {
+          A[r][c] *= y[c];
+          m = fmax(m, fabs(A[r][c]));
+        }
+        double inv = 1.0 / m;
+#pragma unroll
+        for (int c = 0; c < 5; ++c) A[r][c] *= inv;
+        b[r] *= inv;
       }
-      double inv = 1.0 / m;
-#pragma unroll
-      for (int c = 0; c < 5; ++c) A[r][c] *= inv;
-      b[r] *= inv;
+      ok = solve5<false>(A, b, d);
     }
-    bool ok = solve5<MIXED>(A, b, d);
 #pragma unroll
     for (int r = 0; r < 5; ++r) {
       if (!(d[r] > -1.0)) ok = false;

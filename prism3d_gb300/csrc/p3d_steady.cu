@@ -139,6 +139,7 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   p.t_init = t_init; p.f_nano = 1.0; p.e_g = 0.1;
   p.sigma_nano = h2_sigmas[0]; p.sigma_lc = h2_sigmas[1]; p.sigma_sil = h2_sigmas[2];
   p.w_chem = 0.5; p.w_t = 0.5; p.chem_rtol = 1e-12; p.therm_tol = 1e-12;
+  p.therm_tol_mixed = 1e-10;
   p.chem_max_iter = 200; p.therm_max_iter = 80; p.n_rays = (int)n_rays;
   p.h2_implicit = 0;
   p.pe = PeGrid{log_psi_min, log_psi_step, eg_min, eg_step, (int)n_psi, (int)n_eg};
@@ -226,6 +227,10 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   if (e == cudaSuccess)
     e = launch_pe_condense(tab, (int)n_bins, p.pe, bins, bins + n_bins, bins + 2 * n_bins,
                            s->a_nano, s->a_rest, str);
+  if (e == cudaSuccess) {
+    ss_bisect_table_kernel<<<1, 32, 0, str>>>();
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(str);
   if (e != cudaSuccess) { delete h; return cuda_fail(e, "steady create"); }
   *out = h;
@@ -282,6 +287,7 @@ int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, in
   par.count_thr[1] = tol;
   par.count_thr[2] = tol * 0.01;
   par.quiet_tol = tol * 0.01;
+  par.quiet_in_tol = tol * 0.1;
   auto conv = [&](const double* hrow) {
     return hrow[0] < tol || (double)hrow[4] <= (double)n_allow;
   };
@@ -290,10 +296,11 @@ int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, in
   if (stop > kMaxHist) return set_error(P3D_EINVAL, "iteration history full: reset first");
   bool done = false;
   cudaError_t e;
-  if (!mixed) {
-    // plain path: launch, synchronise, test -- once per iteration
+  if (!mixed || max_outer < kGraphIters) {
+    // plain path (and short mixed runs): launch, synchronise, test -- once
+    // per iteration
     while (it < stop && !done) {
-      int rc = launch_iteration(s, false, par, str);
+      int rc = launch_iteration(s, mixed != 0, par, str);
       if (rc) return rc;
       e = cudaMemcpyAsync(s->hist_host + kHistCols * it, s->hist + kHistCols * it,
                           sizeof(double) * kHistCols, cudaMemcpyDeviceToHost, str);
@@ -432,6 +439,7 @@ int p3d_steady_kernel_times(p3d_steady_t* h, int reps, double* ms4) {
   SteadyParams par = s->par;
   par.count_thr[0] = par.count_thr[1] = par.count_thr[2] = 1.0;
   par.quiet_tol = 0.0;  // no compaction: every cell solved
+  par.quiet_in_tol = 0.0;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -471,6 +479,48 @@ int p3d_steady_kernel_times(p3d_steady_t* h, int reps, double* ms4) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  return P3D_OK;
+}
+
+// Live FP64 FMA throughput of the current device: 8 independent DFMA chains
+// per thread, 2 flops per DFMA, timed with CUDA events.
+__global__ void fp64_peak_kernel(double* out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-9 + k;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+
+int p3d_fp64_peak_tflops(double* tflops) {
+  if (!tflops) return set_error(P3D_EINVAL, "null argument");
+  DeviceState* st;
+  int rc = get_state(&st);
+  if (rc) return rc;
+  int err;
+  double* dummy = (double*)st->slot(20, 64, &err);
+  if (err) return err;
+  const int blocks = st->sms * 4, threads = 256, iters = 4096;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  fp64_peak_kernel<<<blocks, threads, 0, st->stream>>>(dummy, 64, 0.999999, 1e-7);
+  cudaEventRecord(e0, st->stream);
+  fp64_peak_kernel<<<blocks, threads, 0, st->stream>>>(dummy, iters, 0.999999, 1e-7);
+  cudaEventRecord(e1, st->stream);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return cuda_fail(e, "fp64 peak probe");
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
   return P3D_OK;
 }
 

@@ -34,11 +34,13 @@ struct SteadyParams {
   double zeta0, x_c_total, x_o_total, x_hcop, t_init, f_nano, e_g;
   double sigma_nano, sigma_lc, sigma_sil;
   double w_chem, w_t, chem_rtol, therm_tol;
+  double therm_tol_mixed;  // thermal-root tolerance of the mixed path
   double theta2;  // T_u of CO J = 1 (the ladder spacing 2 h B / k)
   int chem_max_iter, therm_max_iter, n_rays;
   int h2_implicit;  // 1: the cell's own H2 half layer is solved implicitly
   double count_thr[3];  // thresholds of the n_gt counters
-  double quiet_tol;     // mixed path: skip cells quiescent to this level
+  double quiet_tol;     // mixed path: skip cells whose last change was <= this
+  double quiet_in_tol;  // ... and whose inputs moved <= this since
   PeGrid pe;
   LineParams lines;
 };

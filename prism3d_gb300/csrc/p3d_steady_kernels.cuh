@@ -35,6 +35,27 @@ namespace p3d {
 __constant__ CoLevel c_co_ss[40];
 __constant__ float c_lines32[20];
 __constant__ float c_co32[200];
+// FP64 geometric-bisection tree of [10, 1e5] K: node k (1..1023) holds
+// sqrt(lo * hi) of its bracket, children 2k (net <= 0) and 2k + 1.
+__device__ double g_bisect_mid[1024];
+
+__global__ void ss_bisect_table_kernel() {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double lo[1024], hi[1024];
+  lo[1] = 10.0;
+  hi[1] = 1e5;
+  for (int k = 1; k < 1024; ++k) {
+    double m = sqrt(lo[k] * hi[k]);
+    g_bisect_mid[k] = m;
+    if (2 * k + 1 < 1024) {
+      lo[2 * k] = lo[k];
+      hi[2 * k] = m;
+      lo[2 * k + 1] = m;
+      hi[2 * k + 1] = hi[k];
+    }
+  }
+  g_bisect_mid[0] = 0.0;
+}
 
 // ----------------------------------------------------------------- setup
 __global__ void __launch_bounds__(kThreads)
@@ -218,8 +239,12 @@ __device__ __forceinline__ double t_update(double t_in, double G, double w_t, do
 }
 
 // ----------------------------------------------------------- cell kernel
+#ifndef P3D_CELL_MINBLOCKS
+#define P3D_CELL_MINBLOCKS 1
+#endif
+
 template <bool MIXED>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, P3D_CELL_MINBLOCKS)
 ss_cell_kernel(int64_t n, SteadyDev d, SteadyParams p, const SteadyGlobals* __restrict__ g_in,
                SteadyGlobals* g_out, const double* __restrict__ a_nano,
                const double* __restrict__ a_rest) {
@@ -233,12 +258,13 @@ ss_cell_kernel(int64_t n, SteadyDev d, SteadyParams p, const SteadyGlobals* __re
        i += (int64_t)gridDim.x * blockDim.x) {
     const double uh2 = d.u_h2[i], uco = d.u_co[i];
     if (MIXED && iter > 2) {
-      // compaction: a cell whose last solve changed nothing (to quiet_tol)
-      // and whose inputs have not moved since is its own fixed point
-      const double q = p.quiet_tol;
-      if (d.chg_last[i] <= q && fabs(uh2 - d.u_h2_last[i]) <= q * fabs(uh2) &&
-          fabs(uco - d.u_co_last[i]) <= q * fabs(uco) &&
-          fabs(b_dop - d.b_last[i]) <= q * b_dop)
+      // compaction: a cell whose last solve changed it by <= quiet_tol and
+      // whose inputs (columns, Doppler width) have moved by <= quiet_in_tol
+      // since is at its fixed point to ~tol / 10
+      const double q = p.quiet_tol, qi = p.quiet_in_tol;
+      if (d.chg_last[i] <= q && fabs(uh2 - d.u_h2_last[i]) <= qi * fabs(uh2) &&
+          fabs(uco - d.u_co_last[i]) <= qi * fabs(uco) &&
+          fabs(b_dop - d.b_last[i]) <= qi * b_dop)
         continue;
     }
     ++my_active;
@@ -306,7 +332,8 @@ ss_cell_kernel(int64_t n, SteadyDev d, SteadyParams p, const SteadyGlobals* __re
     c.n_c_nh = x[3] * nh;
     int tst = 0, nev = 0;
     double troot = MIXED ? root_mixed(c, p.lines, c_co_ss, p.theta2, c_lines32, c_co32,
-                                      p.therm_tol, p.therm_max_iter, d.t_root[i], &tst, &nev)
+                                      g_bisect_mid, p.therm_tol_mixed, p.therm_max_iter,
+                                      d.t_root[i], &tst, &nev)
                          : root_plain(c, p.lines, c_co_ss, p.theta2, p.therm_tol,
                                       p.therm_max_iter, &tst, &nev);
     my_evals += (unsigned long long)nev;

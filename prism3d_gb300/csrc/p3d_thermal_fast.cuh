@@ -241,25 +241,29 @@ __device__ __forceinline__ double root_plain(const ThermalCtx& c, const LinePara
   return t;
 }
 
-// Mixed root: the same 10 bisection decisions (midpoints in FP64; a sign is
-// taken from the FP32 evaluation when certified, else from FP64), so the
-// bracket equals the plain path's.  A previous root inside the bracket is
-// accepted when the FP64 sign changes within tol of it (warm start);
-// otherwise Newton starts from it or from a few FP32 Newton steps,
-// finished in FP64: each step uses an FP64 value and the FP32 central
-// difference slope, keeps the bracket with FP64 signs and bisects in FP64
-// when a step leaves it.  Converged as root_plain.
+// Mixed root: the same 10 bisection decisions as root_plain (the midpoints
+// come from `mid_tab`, the FP64 bisection tree: node k has children 2k, 2k+1;
+// a sign is taken from the FP32 evaluation when certified, else from FP64),
+// so the bracket equals the plain path's.  Start: the previous root when it
+// lies in the bracket (warm start), else a few FP32 Newton steps.  Finish:
+// up to three FP64 Newton steps with the FP32 central-difference slope
+// (step 1e-3 T, relative error ~1e-3), done once a step stays in the bracket
+// and moves T by at most 1e-8 T (the slope error then bounds the remaining
+// error by ~1e-11 T); else a two-point FP64 check for a jump of the net
+// heating at T, else the safeguarded FP64 iteration of root_plain to tol.
 __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LineParams& lp,
                                              const CoLevel* __restrict__ co, double theta2,
                                              const float* __restrict__ lines32,
-                                             const float* __restrict__ co32, double tol,
+                                             const float* __restrict__ co32,
+                                             const double* __restrict__ mid_tab, double tol,
                                              int max_it, double t_warm, int* status, int* n64) {
   double K;
   const ThermalCtx32 f32 = make_ctx32(c, lp, co, &K);
   double t_lo = 10.0, t_hi = 1e5;
   int evals = 0;
+  int node = 1;
   for (int k = 0; k < 10; ++k) {
-    double t_mid = sqrt(t_lo * t_hi);
+    double t_mid = __ldg(mid_tab + node);
     float S;
     float v = net_heating32(t_mid, f32, lines32, co32, co, &S);
     bool pos;
@@ -269,26 +273,11 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LinePara
       pos = net_heating_fast64(t_mid, c, lp, co, theta2) > 0.0;
       ++evals;
     }
-    if (pos) t_lo = t_mid; else t_hi = t_mid;
+    if (pos) { t_lo = t_mid; node = 2 * node + 1; } else { t_hi = t_mid; node = 2 * node; }
   }
   double t;
   if (t_warm > t_lo && t_warm < t_hi) {
-    // warm start: a sign change within tol of the previous root ends the
-    // search (smooth roots and jumps alike) in two FP64 evaluations
-    double a = t_warm * (1.0 - 0.5 * tol), b = t_warm * (1.0 + 0.5 * tol);
-    double fa = net_heating_fast64(a, c, lp, co, theta2);
-    double fb = net_heating_fast64(b, c, lp, co, theta2);
-    evals += 2;
-    if (fa > 0.0 && !(fb > 0.0)) {
-      *status = 0;
-      *n64 = evals;
-      return t_warm;
-    }
-    double lo2 = t_lo, hi2 = t_hi;
-    if (fa > 0.0) lo2 = fmax(lo2, a); else hi2 = fmin(hi2, a);
-    if (fb > 0.0) lo2 = fmax(lo2, b); else hi2 = fmin(hi2, b);
-    if (lo2 < hi2) { t_lo = lo2; t_hi = hi2; }
-    t = (t_warm > t_lo && t_warm < t_hi) ? t_warm : sqrt(t_lo * t_hi);
+    t = t_warm;
   } else {
     t = sqrt(t_lo * t_hi);
     for (int k = 0; k < 4; ++k) {  // FP32 Newton inside the bracket
@@ -304,12 +293,46 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LinePara
       if (small) break;
     }
   }
-  // FP64 finish
   float S1, S2;
   double h = 1e-3 * t;
   double slope = (double)(net_heating32(t + h, f32, lines32, co32, co, &S1) -
                           net_heating32(t - h, f32, lines32, co32, co, &S2)) / (2.0 * h) / K;
   *status = 1;
+  for (int k = 0; k < 3; ++k) {  // up to three FP64 Newton steps
+    double f = net_heating_fast64(t, c, lp, co, theta2);
+    ++evals;
+    if (f > 0.0) t_lo = fmax(t_lo, t); else t_hi = fmin(t_hi, t);
+    if (f == 0.0) {
+      *status = 0;
+      *n64 = evals;
+      return t;
+    }
+    double tn = t - f / slope;
+    if (!(slope < 0.0 && tn > t_lo && tn < t_hi)) break;
+    bool small = fabs(tn - t) <= 1e-8 * t;
+    t = tn;
+    if (small) {
+      *status = 0;
+      *n64 = evals;
+      return t;
+    }
+  }
+  {  // jump of the net heating at t: sign change across t (1 +- tol / 2)
+    double a = t * (1.0 - 0.5 * tol), b = t * (1.0 + 0.5 * tol);
+    double fa = net_heating_fast64(a, c, lp, co, theta2);
+    double fb = net_heating_fast64(b, c, lp, co, theta2);
+    evals += 2;
+    if (fa > 0.0 && !(fb > 0.0)) {
+      *status = 0;
+      *n64 = evals;
+      return t;
+    }
+    double lo2 = t_lo, hi2 = t_hi;
+    if (fa > 0.0) lo2 = fmax(lo2, a); else hi2 = fmin(hi2, a);
+    if (fb > 0.0) lo2 = fmax(lo2, b); else hi2 = fmin(hi2, b);
+    if (lo2 < hi2) { t_lo = lo2; t_hi = hi2; }
+    if (!(t > t_lo && t < t_hi)) t = sqrt(t_lo * t_hi);
+  }
   double dx_old = t_hi - t_lo, dx = dx_old;
   for (int k = 0; k < max_it; ++k) {
     double f = net_heating_fast64(t, c, lp, co, theta2);

@@ -77,6 +77,9 @@ WORKLOADS = {
     "slab128": (lambda seed=1: orion_bar_slab(128, seed=seed), 2.6e4, 2, 2e-16),
     "cube32": (lambda seed=1: lognormal_cube(32, 3e4, 1.0, seed), 1e4, 1, 2e-16),
     "slab256": (lambda seed=1: cored_slab(256, seed=seed), 2.6e4, 2, 5e-16),
+    # the 128^3 slab's recipe on 96^3 cells: state (~0.27 GB) above L2, small
+    # enough for a profiler capture
+    "slab96": (lambda seed=1: orion_bar_slab(96, seed=seed), 2.6e4, 2, 2e-16),
 }
 
 

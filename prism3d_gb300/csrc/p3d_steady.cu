@@ -83,18 +83,23 @@ static int launch_iteration(SteadySolver* s, bool mixed, const SteadyParams& par
   ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(s->n, d.t_gas, s->parts);
   ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, s->n, s->glob);
   unsigned grid = grid_for(s->n, s->st->sms, 4);
-  if (mixed)
-    ss_cell_kernel<true><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->glob,
-                                                     s->a_nano, s->a_rest);
-  else
-    ss_cell_kernel<false><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->glob,
-                                                      s->a_nano, s->a_rest);
+  if (mixed) {
+    ss_mark_kernel<true><<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(s->n, d, par,
+                                                                              s->glob);
+    ss_chem_kernel<true><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->a_nano,
+                                                     s->a_rest);
+    ss_thermal_kernel<true><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob);
+  } else {
+    ss_chem_kernel<false><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->a_nano,
+                                                      s->a_rest);
+    ss_thermal_kernel<false><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob);
+  }
   ss_record_kernel<<<1, 32, 0, str>>>(s->glob, s->hist, kMaxHist);
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? P3D_OK : cuda_fail(e, "steady iteration launch");
 }
 
-constexpr int kLaunchesPerIteration = 7;
+constexpr int kLaunchesPerIteration = 9;  // mixed; the plain path launches 8
 
 }  // namespace p3d
 
@@ -151,12 +156,13 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   double** dbl[] = {&s->dens, &d.g0, &d.av, &d.nh_col, &s->nh2_full, &s->nco_full, &d.ds,
                     &d.kpd0, &d.uv0, &d.kci, &d.kco0, &d.hci0, &d.zeta, &d.td_rad, &d.t_gas,
                     &d.x_hi, &d.x_h2, &d.x_cp, &d.x_c, &d.x_co, &d.x_o, &d.x_e, &d.u_h2,
-                    &d.u_co, &d.t_prev, &d.r_prev, &d.t_lo, &d.t_hi, &d.span, &d.t_root, &d.u_h2_last, &d.u_co_last, &d.b_last, &d.chg_last, &d.fh2,
+                    &d.u_co, &d.t_prev, &d.r_prev, &d.t_lo, &d.t_hi, &d.span, &d.t_root, &d.u_h2_last, &d.u_co_last, &d.b_last, &d.chg_last, &d.rh2_cell, &d.chg_spec, &d.fh2,
                     &d.gamma_pe, &d.t_dust, &s->scratch};
   for (double** q : dbl)
     if ((rc = s->alloc(q, n))) { delete h; return rc; }
   d.dens = s->dens;
-  if ((rc = s->alloc(&d.ray, n)) || (rc = s->alloc(&d.fam, n)) || (rc = s->alloc(&d.flags, n))) {
+  if ((rc = s->alloc(&d.ray, n)) || (rc = s->alloc(&d.fam, n)) || (rc = s->alloc(&d.flags, n)) ||
+      (rc = s->alloc(&d.list, n))) {
     delete h;
     return rc;
   }
@@ -306,7 +312,7 @@ int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, in
                           sizeof(double) * kHistCols, cudaMemcpyDeviceToHost, str);
       if (e == cudaSuccess) e = cudaStreamSynchronize(str);
       if (e != cudaSuccess) return cuda_fail(e, "plain iteration");
-      s->launches += kLaunchesPerIteration;
+      s->launches += kLaunchesPerIteration - (mixed ? 0 : 1);
       s->last_dmax = s->hist_host[kHistCols * it];
       bool c = conv(s->hist_host + kHistCols * it);
       ++it;
@@ -459,11 +465,16 @@ int p3d_steady_kernel_times(p3d_steady_t* h, int reps, double* ms4) {
         ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(s->n, d.t_gas, s->parts);
         ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, s->n, s->glob);
       } else if (which == 2) {
-        ss_cell_kernel<true><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->glob,
-                                                         s->a_nano, s->a_rest);
+        ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, s->n, s->glob);
+        ss_mark_kernel<true><<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(s->n, d, par,
+                                                                                  s->glob);
+        ss_chem_kernel<true><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->a_nano,
+                                                         s->a_rest);
+        ss_thermal_kernel<true><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob);
       } else {
-        ss_cell_kernel<false><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->glob,
-                                                          s->a_nano, s->a_rest);
+        ss_chem_kernel<false><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->a_nano,
+                                                          s->a_rest);
+        ss_thermal_kernel<false><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob);
       }
     }
     cudaEventRecord(e1, str);

@@ -25,6 +25,10 @@ struct SteadyDev {
   double* t_root;
   // inputs at the last solve and the change it made (mixed-path compaction)
   double *u_h2_last, *u_co_last, *b_last, *chg_last;
+  // cells solved this iteration (dense list) and values passed from the
+  // chemistry kernel to the thermal kernel
+  int32_t* list;
+  double *rh2_cell, *chg_spec;
   // diagnostics of the last iteration
   double *fh2, *gamma_pe, *t_dust;
   int32_t* flags;
@@ -52,7 +56,7 @@ struct SteadyGlobals {
   unsigned long long evals64;  // FP64 net-heating evaluations
   unsigned int chem_fail, therm_fail;
   unsigned int n_gt[3];  // cells with relative change > count_thr[k]
-  unsigned int n_active;  // cells solved this iteration
+  unsigned int n_active;  // cells solved this iteration (length of the list)
   int iter;
 };
 

@@ -239,35 +239,55 @@ __device__ __forceinline__ double t_update(double t_in, double G, double w_t, do
 }
 
 // ----------------------------------------------------------- cell kernel
-#ifndef P3D_CELL_MINBLOCKS
-#define P3D_CELL_MINBLOCKS 1
-#endif
-
+// ------------------------------------------------------------ worklist
+// A cell is solved this iteration unless (mixed path, from the fourth
+// iteration on) its last solve changed it by <= quiet_tol and its inputs --
+// selected-ray columns, Doppler width -- have moved by <= quiet_in_tol since:
+// then it is at its fixed point to ~tol / 10 and keeps its state.  Solved
+// cells are appended to a dense list (one atomic per warp), so the chemistry
+// and thermal kernels run full warps of active cells.
 template <bool MIXED>
-__global__ void __launch_bounds__(kThreads, P3D_CELL_MINBLOCKS)
-ss_cell_kernel(int64_t n, SteadyDev d, SteadyParams p, const SteadyGlobals* __restrict__ g_in,
-               SteadyGlobals* g_out, const double* __restrict__ a_nano,
-               const double* __restrict__ a_rest) {
-  const double b_dop = g_in->b_dop;
-  const int iter = g_in->iter;
-  double my_max = 0.0;
-  unsigned int my_gt[3] = {0u, 0u, 0u};
-  unsigned int my_active = 0u;
-  unsigned long long my_evals = 0ull;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const double uh2 = d.u_h2[i], uco = d.u_co[i];
-    if (MIXED && iter > 2) {
-      // compaction: a cell whose last solve changed it by <= quiet_tol and
-      // whose inputs (columns, Doppler width) have moved by <= quiet_in_tol
-      // since is at its fixed point to ~tol / 10
+__global__ void __launch_bounds__(kThreads)
+ss_mark_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
+  const double b_dop = g->b_dop;
+  const int iter = g->iter;
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); base < n;
+       base += stride) {
+    const int64_t i = base + lane;
+    bool active = i < n;
+    if (active && MIXED && iter > 2) {
       const double q = p.quiet_tol, qi = p.quiet_in_tol;
+      const double uh2 = d.u_h2[i], uco = d.u_co[i];
       if (d.chg_last[i] <= q && fabs(uh2 - d.u_h2_last[i]) <= qi * fabs(uh2) &&
           fabs(uco - d.u_co_last[i]) <= qi * fabs(uco) &&
           fabs(b_dop - d.b_last[i]) <= qi * b_dop)
-        continue;
+        active = false;
     }
-    ++my_active;
+    const unsigned m = __ballot_sync(0xffffffffu, active);
+    if (m) {
+      unsigned pos = 0;
+      if (lane == 0) pos = atomicAdd(&g->n_active, (unsigned)__popc(m));
+      pos = __shfl_sync(0xffffffffu, pos, 0);
+      if (active) d.list[pos + __popc(m & ((1u << lane) - 1u))] = (int32_t)i;
+    }
+  }
+}
+
+// Dust coupling, rates, steady-state chemistry, damping.  Cells k < count of
+// the list (plain path: every cell, no list).
+template <bool MIXED>
+__global__ void __launch_bounds__(kThreads)
+ss_chem_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g,
+               const double* __restrict__ a_nano, const double* __restrict__ a_rest) {
+  const double b_dop = g->b_dop;
+  const int iter = g->iter;
+  const int64_t count = MIXED ? (int64_t)g->n_active : n;
+  unsigned int my_fail = 0u;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = MIXED ? (int64_t)d.list[k] : k;
     const double nh = d.dens[i];
     const double tg = d.t_gas[i];
     const double xe0 = d.x_e[i];
@@ -289,47 +309,81 @@ ss_cell_kernel(int64_t n, SteadyDev d, SteadyParams p, const SteadyGlobals* __re
     cc.kpd0 = d.kpd0[i];
     cc.kco0 = d.kco0[i];
     cc.kco_cr = 6.0 * zeta;
-    cc.u_h2 = uh2;
-    cc.u_co = uco;
+    cc.u_h2 = d.u_h2[i];
+    cc.u_co = d.u_co[i];
     cc.ds = p.h2_implicit ? d.ds[i] : 0.0;
     cc.b_dop = b_dop;
     chem_prepare(cc);
     double y[5];
 #pragma unroll
-    for (int k = 0; k < 5; ++k) y[k] = fmax(y_old[k], 1e-30);
+    for (int c = 0; c < 5; ++c) y[c] = fmax(y_old[c], 1e-30);
     double fh2 = 1.0;
     int citers = 0;
     int cst = chem_steady_cell<MIXED>(cc, y, p.chem_max_iter, p.chem_rtol, 4.0, &fh2, &citers);
-    const double x_o = fmax(p.x_o_total - y[4], 1e-30);
-    const double x_e = fmax(y[2] + p.x_hcop, 1e-30);
+    my_fail += (unsigned)cst;
     double x[5];
-    if (iter > 0 && p.w_chem > 0.0) {
+    const bool damp = iter > 0 && p.w_chem > 0.0;
+    double m = 0.0;
 #pragma unroll
-      for (int k = 0; k < 5; ++k) x[k] = p.w_chem * y_old[k] + (1.0 - p.w_chem) * y[k];
-    } else {
-#pragma unroll
-      for (int k = 0; k < 5; ++k) x[k] = y[k];
+    for (int c = 0; c < 5; ++c) {
+      x[c] = damp ? p.w_chem * y_old[c] + (1.0 - p.w_chem) * y[c] : y[c];
+      m = fmax(m, fabs(x[c] - y_old[c]) / fmax(y_old[c], 1e-20));
     }
-    // thermal context (solver_3d.py:693-754)
+    d.x_hi[i] = x[0];
+    d.x_h2[i] = x[1];
+    d.x_cp[i] = x[2];
+    d.x_c[i] = x[3];
+    d.x_co[i] = x[4];
+    d.x_o[i] = fmax(p.x_o_total - y[4], 1e-30);
+    d.x_e[i] = fmax(y[2] + p.x_hcop, 1e-30);
+    d.fh2[i] = fh2;
+    d.gamma_pe[i] = gpe;
+    d.t_dust[i] = td;
+    d.rh2_cell[i] = rh2;
+    d.chg_spec[i] = m;
+  }
+  for (int o = 16; o > 0; o >>= 1) my_fail += __shfl_xor_sync(0xffffffffu, my_fail, o);
+  if ((threadIdx.x & 31) == 0 && my_fail) atomicAdd(&g->chem_fail, my_fail);
+}
+
+// Thermal context (solver_3d.py:693-754), thermal root, per-cell T update,
+// convergence measure.
+template <bool MIXED>
+__global__ void __launch_bounds__(kThreads)
+ss_thermal_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
+  const double b_dop = g->b_dop;
+  const int64_t count = MIXED ? (int64_t)g->n_active : n;
+  double my_max = 0.0;
+  unsigned int my_gt[3] = {0u, 0u, 0u};
+  unsigned int my_fail = 0u;
+  unsigned long long my_evals = 0ull;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = MIXED ? (int64_t)d.list[k] : k;
+    const double nh = d.dens[i];
+    const double tg = d.t_gas[i];
+    const double x0 = d.x_hi[i], x1 = d.x_h2[i], x3 = d.x_c[i];
+    const double zeta = d.zeta[i];
+    const double rh2 = d.rh2_cell[i];
     ThermalCtx c;
-    const double uv = d.uv0[i] * fh2;
-    double gf = gpe;
-    gf += 3.3e-11 * uv * x[1] * nh * (0.4 * kEVtoErg);
-    gf += rh2 * x[0] * (nh * nh) * (1.5 * kEVtoErg);
-    gf += 3.0e-10 * uv * x[1] * nh * (2.0 * kEVtoErg) * (nh / (nh + 3e4));
-    gf += zeta * (x[0] + 2.0 * x[1]) * nh * (20.0 * kEVtoErg);
-    gf += d.hci0[i] * x[3] * nh * kEVtoErg;
+    const double uv = d.uv0[i] * d.fh2[i];
+    double gf = d.gamma_pe[i];
+    gf += 3.3e-11 * uv * x1 * nh * (0.4 * kEVtoErg);
+    gf += rh2 * x0 * (nh * nh) * (1.5 * kEVtoErg);
+    gf += 3.0e-10 * uv * x1 * nh * (2.0 * kEVtoErg) * (nh / (nh + 3e4));
+    gf += zeta * (x0 + 2.0 * x1) * nh * (20.0 * kEVtoErg);
+    gf += d.hci0[i] * x3 * nh * kEVtoErg;
     c.gamma_fixed = gf;
-    const double mu = x[1] > 0.5 ? 2.0 : 1.0;
+    const double mu = x1 > 0.5 ? 2.0 : 1.0;
     c.gg_coeff = 2.0 * 0.35 * 1e-21 * (nh * nh) * sqrt(8.0 * kKBoltz / (kPi * mu * kMH)) * kKBoltz;
-    c.t_dust = td;
-    c.n_e = x_e * nh;
-    c.n_hi = x[0] * nh;
-    c.n_h2 = x[1] * nh;
-    c.n_co = x[4] * nh;
-    c.n_cp_nh = x[2] * nh;
-    c.n_o_nh = x_o * nh;
-    c.n_c_nh = x[3] * nh;
+    c.t_dust = d.t_dust[i];
+    c.n_e = d.x_e[i] * nh;
+    c.n_hi = x0 * nh;
+    c.n_h2 = x1 * nh;
+    c.n_co = d.x_co[i] * nh;
+    c.n_cp_nh = d.x_cp[i] * nh;
+    c.n_o_nh = d.x_o[i] * nh;
+    c.n_c_nh = x3 * nh;
     int tst = 0, nev = 0;
     double troot = MIXED ? root_mixed(c, p.lines, c_co_ss, p.theta2, c_lines32, c_co32,
                                       g_bisect_mid, p.therm_tol_mixed, p.therm_max_iter,
@@ -337,55 +391,40 @@ ss_cell_kernel(int64_t n, SteadyDev d, SteadyParams p, const SteadyGlobals* __re
                          : root_plain(c, p.lines, c_co_ss, p.theta2, p.therm_tol,
                                       p.therm_max_iter, &tst, &nev);
     my_evals += (unsigned long long)nev;
-    d.t_root[i] = troot;
+    my_fail += (unsigned)tst;
     double tp = d.t_prev[i], rp = d.r_prev[i], lo = d.t_lo[i], hi = d.t_hi[i], sp = d.span[i];
     double tn = t_update(tg, troot, p.w_t, tp, rp, lo, hi, sp);
-    // convergence measure: largest relative change of T and the species
-    double m = fabs(tn - tg) / tg;
-#pragma unroll
-    for (int k = 0; k < 5; ++k) m = fmax(m, fabs(x[k] - y_old[k]) / fmax(y_old[k], 1e-20));
+    double m = fmax(d.chg_spec[i], fabs(tn - tg) / tg);
     if (!(m == m)) m = INFINITY;
     my_max = fmax(my_max, m);
     my_gt[0] += m > p.count_thr[0];
     my_gt[1] += m > p.count_thr[1];
     my_gt[2] += m > p.count_thr[2];
-    d.u_h2_last[i] = uh2;
-    d.u_co_last[i] = uco;
-    d.b_last[i] = b_dop;
-    d.chg_last[i] = m;
-    if (cst) atomicAdd(&g_out->chem_fail, 1u);
-    if (tst) atomicAdd(&g_out->therm_fail, 1u);
-    d.x_hi[i] = x[0];
-    d.x_h2[i] = x[1];
-    d.x_cp[i] = x[2];
-    d.x_c[i] = x[3];
-    d.x_co[i] = x[4];
-    d.x_o[i] = x_o;
-    d.x_e[i] = x_e;
+    d.t_root[i] = troot;
     d.t_gas[i] = tn;
     d.t_prev[i] = tp;
     d.r_prev[i] = rp;
     d.t_lo[i] = lo;
     d.t_hi[i] = hi;
     d.span[i] = sp;
-    d.fh2[i] = fh2;
-    d.gamma_pe[i] = gpe;
-    d.t_dust[i] = td;
+    d.u_h2_last[i] = d.u_h2[i];
+    d.u_co_last[i] = d.u_co[i];
+    d.b_last[i] = b_dop;
+    d.chg_last[i] = m;
   }
-  block_max_atomic(my_max, &g_out->dmax_bits);
-  // counters: warp sums, one atomic per warp
+  block_max_atomic(my_max, &g->dmax_bits);
   for (int o = 16; o > 0; o >>= 1) {
     my_evals += __shfl_xor_sync(0xffffffffu, my_evals, o);
-    my_active += __shfl_xor_sync(0xffffffffu, my_active, o);
+    my_fail += __shfl_xor_sync(0xffffffffu, my_fail, o);
 #pragma unroll
     for (int k = 0; k < 3; ++k) my_gt[k] += __shfl_xor_sync(0xffffffffu, my_gt[k], o);
   }
   if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&g_out->evals64, my_evals);
-    if (my_active) atomicAdd(&g_out->n_active, my_active);
+    atomicAdd(&g->evals64, my_evals);
+    if (my_fail) atomicAdd(&g->therm_fail, my_fail);
 #pragma unroll
     for (int k = 0; k < 3; ++k)
-      if (my_gt[k]) atomicAdd(&g_out->n_gt[k], my_gt[k]);
+      if (my_gt[k]) atomicAdd(&g->n_gt[k], my_gt[k]);
   }
 }
 
@@ -418,7 +457,7 @@ __global__ void ss_record_kernel(SteadyGlobals* g, double* hist, int max_hist) {
       h[5] = (double)g->n_gt[2];
       h[6] = (double)g->evals64;
       h[7] = g->t_mean;
-      h[8] = (double)g->n_active;
+      h[8] = (double)g->n_active;  // plain path: 0 (no list; every cell solved)
     }
     g->iter = it + 1;
   }

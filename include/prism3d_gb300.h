@@ -274,6 +274,79 @@ int p3d_steady_launch_count(p3d_steady_t *s, int64_t *out);
  * plain per-cell kernel with every cell solved.  Advances the state. */
 int p3d_steady_kernel_times(p3d_steady_t *s, int reps, double *ms4);
 
+/* ---------------------------------------------------------------------
+ * Full chemical network, one warp per cell.  The network is data: the
+ * reaction table of build_pdr_network() (prism3d/chemistry/network.py:
+ * 186-896) with the rate laws of ChemistrySolver._rhs
+ * (prism3d/chemistry/solver.py:69-143).
+ *
+ * p3d_network_create   compile a reaction table (host arrays) into a
+ *                      device-resident network on the current device.
+ *   rtype[j]           P3D_RX_* below
+ *   alpha/beta/gamma   the reaction's (alpha, beta, gamma)
+ *   reactants[2 j + m] species index, P3D_NET_UNTRACKED (abundance 0, as
+ *                      the reference treats species it does not track) or
+ *                      P3D_NET_PAH_MINUS (PAH-, from the PAH charge
+ *                      balance of solver.py:76-88)
+ *   products[4 j + m]  species index or P3D_NET_UNTRACKED (ignored)
+ *   shield[j]          1: multiply k by f_shield_H2, 2: by f_shield_CO
+ *   element_counts     n_elements x n_species atoms of each element
+ *   charge[i]          species charge; the electron row of the steady state
+ *                      is y[e_index] = sum of cations (charge x abundance)
+ *   reference_layout   1 if the species are solver.py:28-36's 31 in that
+ *                      order (enables post-processing; c_total, o_total are
+ *                      then the gas-phase C and O abundances it uses)
+ *   Limits: n_species <= 32, n_reactions <= 96, n_elements <= 8, each
+ *   element needs a species made of it alone.
+ * p3d_network_rhs      dy/dt of ChemistrySolver._rhs for n states.
+ *   cond               n x 7: n_H, T, G0, A_V, zeta_CR, f_shield_H2,
+ *                      f_shield_CO (the reference's positional arguments)
+ *   x, dxdt            n x n_species
+ * p3d_network_steady   steady state for n cells, x in/out (n x n_species):
+ *                      Newton / pseudo-transient continuation in relative
+ *                      variables with the element totals of the input state
+ *                      and charge neutrality as constraints; converged when,
+ *                      for every abundance above 1e-25, the relative change
+ *                      is <= rtol and the residual <= rtol of the species'
+ *                      production + destruction.
+ *                      mixed = 1: FP32 factorisation with two FP64-residual
+ *                      refinements (F, J and the test stay FP64).  post = 1
+ *                      (reference layout only): apply solver.py:227-281 and
+ *                      :345-388 to the result, as solve_steady_state does.
+ *                      status[i] 0 = converged (may be NULL), iters[i] the
+ *                      Newton iterations (may be NULL).  The host-buffer
+ *                      form returns P3D_ECONVERGE (results kept) if a cell
+ *                      did not converge in max_iter iterations.
+ * No counterpart entry point in the reference (its solver runs SciPy BDF per
+ * cell in Python).
+ * ------------------------------------------------------------------- */
+#define P3D_RX_TWO_BODY 0      /* k = a (Tc/300)^b exp(-g/Tc), Tc = clip(T, 10, 41000); r = k xA xB n_H */
+#define P3D_RX_PHOTO 1         /* k = a G0 exp(-g A_V) [x f_shield]; r = k xA */
+#define P3D_RX_CR 2            /* k = a zeta_CR; r = k xA */
+#define P3D_RX_GRAIN_SURFACE 3 /* k = a (T/300)^b; r = k x_H n_H / 2 */
+#define P3D_NET_UNTRACKED (-1)
+#define P3D_NET_PAH_MINUS (-2)
+
+typedef struct p3d_network p3d_network_t;
+
+int p3d_network_create(p3d_network_t **out, int32_t n_species, int32_t n_reactions,
+                       const int32_t *rtype, const double *alpha, const double *beta,
+                       const double *gamma, const int32_t *reactants, const int32_t *products,
+                       const int32_t *shield, int32_t n_elements, const double *element_counts,
+                       const int32_t *charge, int32_t e_index, double pah_total,
+                       int32_t reference_layout, double c_total, double o_total);
+int p3d_network_rhs(p3d_network_t *net, int64_t n, const double *cond, const double *x,
+                    double *dxdt);
+int p3d_network_rhs_dev(p3d_network_t *net, int64_t n, const double *cond, const double *x,
+                        double *dxdt, void *stream);
+int p3d_network_steady(p3d_network_t *net, int64_t n, const double *cond, double *x, int32_t mixed,
+                       int32_t post, int32_t max_iter, double rtol, int32_t *status,
+                       int32_t *iters);
+int p3d_network_steady_dev(p3d_network_t *net, int64_t n, const double *cond, double *x,
+                           int32_t mixed, int32_t post, int32_t max_iter, double rtol,
+                           int32_t *status, int32_t *iters, void *stream);
+int p3d_network_destroy(p3d_network_t *net);
+
 #ifdef __cplusplus
 }
 #endif

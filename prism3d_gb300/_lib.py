@@ -15,6 +15,7 @@ _D = ctypes.POINTER(ctypes.c_double)
 _I32 = ctypes.POINTER(ctypes.c_int32)
 _I64 = ctypes.POINTER(ctypes.c_int64)
 _i64 = ctypes.c_int64
+_i32 = ctypes.c_int32
 _f64 = ctypes.c_double
 _vp = ctypes.c_void_p
 
@@ -54,6 +55,13 @@ SIGNATURES = {
     "p3d_steady_elapsed_ms": [_vp, _D],
     "p3d_fp64_peak_tflops": [_D],
     "p3d_steady_kernel_times": [_vp, ctypes.c_int, _D],
+    "p3d_network_create": [ctypes.POINTER(_vp), _i32, _i32, _I32, _D, _D, _D, _I32, _I32, _I32,
+                           _i32, _D, _I32, _i32, _f64, _i32, _f64, _f64],
+    "p3d_network_rhs": [_vp, _i64, _D, _D, _D],
+    "p3d_network_rhs_dev": [_vp, _i64, _D, _D, _D, _vp],
+    "p3d_network_steady": [_vp, _i64, _D, _D, _i32, _i32, _i32, _f64, _I32, _I32],
+    "p3d_network_steady_dev": [_vp, _i64, _D, _D, _i32, _i32, _i32, _f64, _I32, _I32, _vp],
+    "p3d_network_destroy": [_vp],
 }
 _RESTYPES = {"p3d_version": ctypes.c_char_p, "p3d_last_error": ctypes.c_char_p}
 

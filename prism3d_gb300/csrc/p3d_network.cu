@@ -56,6 +56,8 @@ constexpr double kFloor = 1e-30;
 constexpr double kGrowth = 2.0;
 constexpr double kYTest = 1e-25;  // abundances at or below are not tested
 constexpr int kRefine = 2;
+constexpr double kRefineBelow = 0.5;  // refine when the last step was below
+constexpr int kSwitch64 = 100;  // mixed: FP64 factorisation from this iteration on
 
 // Reference species layout (solver.py:28-36).
 enum RefIdx : int {
@@ -194,17 +196,23 @@ __device__ __forceinline__ void eval_f(const Table& T, const Warp& W, int r, dou
   *sc = s;
 }
 
-__device__ __forceinline__ void warp_argmax(double& v, int& p) {
-#pragma unroll
-  for (int off = 16; off; off >>= 1) {
-    const double ov = __shfl_xor_sync(0xffffffffu, v, off);
-    const int op = __shfl_xor_sync(0xffffffffu, p, off);
-    if (ov > v || (ov == v && op < p)) {
-      v = ov;
-      p = op;
-    }
-  }
+// Pivot search: one warp reduction of a 32-bit key per column.  The key is
+// the high word of |a| (FP64: sign, exponent, 20 mantissa bits; FP32: the
+// whole |a|) with its low 5 bits replaced by 31 - lane, so the maximum picks
+// the largest magnitude to 2^-15 relative (FP64) or 2^-18 (FP32) and the
+// lowest lane on ties.  Excluded lanes pass key 0.  Returns the pivot lane,
+// or -1 if every candidate is zero.
+__device__ __forceinline__ int pivot_lane(unsigned int mag_bits, bool cand, int lane) {
+  const unsigned int key = cand ? ((mag_bits & ~31u) | (unsigned int)(31 - lane)) : 0u;
+  const unsigned int m = __reduce_max_sync(0xffffffffu, key);
+  return (m & ~31u) ? 31 - (int)(m & 31u) : -1;
 }
+
+__device__ __forceinline__ unsigned int mag_hi(double a) {
+  return (unsigned int)(__double_as_longlong(a) >> 32) & 0x7fffffffu;
+}
+
+__device__ __forceinline__ unsigned int mag32(float a) { return __float_as_uint(a) & 0x7fffffffu; }
 
 __device__ __forceinline__ double warp_max(double v) {
 #pragma unroll
@@ -217,10 +225,8 @@ __device__ __forceinline__ double warp_max(double v) {
 __device__ bool lu_solve64(Warp& W, int ns, int lane, double b, double* x) {
   int my = lane < ns ? -1 : (1 << 20);
   for (int k = 0; k < ns; ++k) {
-    double v = my < 0 ? fabs(W.A[lane][k]) : -1.0;
-    int p = lane;
-    warp_argmax(v, p);
-    if (!(v > 0.0)) return false;
+    const int p = pivot_lane(my < 0 ? mag_hi(W.A[lane][k]) : 0u, my < 0, lane);
+    if (p < 0) return false;
     if (lane == p) my = k;
     if (lane == 0) W.perm[k] = p;
     const double bp = __shfl_sync(0xffffffffu, b, p);
@@ -248,10 +254,8 @@ __device__ bool lu_solve64(Warp& W, int ns, int lane, double b, double* x) {
 __device__ bool lu_factor32(Warp& W, int ns, int lane, int* my_out) {
   int my = lane < ns ? -1 : (1 << 20);
   for (int k = 0; k < ns; ++k) {
-    double v = my < 0 ? (double)fabsf(W.L[lane][k]) : -1.0;
-    int p = lane;
-    warp_argmax(v, p);
-    if (!(v > 0.0)) return false;
+    const int p = pivot_lane(my < 0 ? mag32(W.L[lane][k]) : 0u, my < 0, lane);
+    if (p < 0) return false;
     if (lane == p) my = k;
     if (lane == 0) W.perm[k] = p;
     const float piv = W.L[p][k];
@@ -400,7 +404,7 @@ __global__ void __launch_bounds__(kWarps * 32)
       for (int i = 0; i < ns; ++i) tot += T.el[lane][i] * W.y[i];
       W.tot[lane] = tot;
     }
-    double inv_dt = 0.0;
+    double inv_dt = 0.0, wprev = 1.0;
     int it = 0;
     bool conv = false;
     while (it < max_iter) {
@@ -457,24 +461,30 @@ __global__ void __launch_bounds__(kWarps * 32)
         d = y - s;
       }
       __syncwarp();
+      // column scaling by y (relative variables), then row scaling by the
+      // power of two at the row's largest magnitude (exact; the largest
+      // entry lands in [1, 2)).  The magnitude scan runs on the high words
+      // and also flags Inf/NaN.
       bool finite = true;
       if (row) {
-        double s = 0.0;
+        unsigned int mx = 0u;
         for (int j = 0; j < ns; ++j) {
           const double a = W.A[lane][j] * W.y[j];
           W.A[lane][j] = a;
-          s = fmax(s, fabs(a));
+          mx = max(mx, mag_hi(a));
         }
-        if (!(s > 0.0)) s = 1.0;
-        const double inv = 1.0 / s;
+        finite = mx < 0x7ff00000u && isfinite(d);
+        double inv = 1.0;
+        if (mx >= 0x00100000u) {
+          const int biased = min(max(2046 - (int)(mx >> 20), 1), 2046);
+          inv = __longlong_as_double((long long)biased << 52);
+        }
         for (int j = 0; j < ns; ++j) {
-          W.A[lane][j] *= inv;
-          finite = finite && isfinite(W.A[lane][j]);
+          const double a = W.A[lane][j] * inv;
+          W.A[lane][j] = a;
+          if (MIXED && it < kSwitch64) W.L[lane][j] = (float)a;
         }
         d *= inv;
-        finite = finite && isfinite(d);
-        if (MIXED)
-          for (int j = 0; j < ns; ++j) W.L[lane][j] = (float)W.A[lane][j];
       }
       const bool res_ok = !ode || fabs(f) <= rtol * sc || y <= kYTest;
       const double lam = warp_max(jd);
@@ -482,12 +492,15 @@ __global__ void __launch_bounds__(kWarps * 32)
       bool ok = __all_sync(0xffffffffu, finite);
       double wr = 0.0;
       if (ok) {
-        if (MIXED) {
+        if (MIXED && it < kSwitch64) {
           int my;
           ok = lu_factor32(W, ns, lane, &my);
           if (ok) {
             wr = (double)lu_apply32(W, ns, lane, my, (float)d);
-            for (int rep = 0; rep < kRefine; ++rep) {
+            // refinement only once the iteration is close to the root: the
+            // pseudo-time steps before do not need an exact direction
+            const int n_ref = wprev < kRefineBelow ? kRefine : 0;
+            for (int rep = 0; rep < n_ref; ++rep) {
               if (row) W.w[lane] = wr;
               __syncwarp();
               double res = d;
@@ -510,6 +523,7 @@ __global__ void __launch_bounds__(kWarps * 32)
         inv_dt = (inv_dt == 0.0) ? lam / 10.0 + 1e-30 : inv_dt * 4.0;
         continue;
       }
+      wprev = warp_max(row && y > kYTest ? fabs(wr) : 0.0);
       if (row) {
         y = fmax(y * (1.0 + fmax(wr, -1.0)), kFloor);
         W.y[lane] = y;

@@ -210,13 +210,14 @@ def run_gb300(args, ws, rank, local):
                 "d2h_bytes_per_step": int(d2h)},
         "plain_fp64": plain,
         "mixed_vs_plain": (value / ws) / plain.get("value", plain.get("value_est")),
-        "roofline": {"kernel": "ss_cell_kernel<mixed> (98% of solve time), every cell solved",
+        "roofline": {"kernel": "ss_mark/chem/thermal_kernel<mixed> (97% of solve time), every "
+                               "cell solved",
                      "bound": "fp64", "achieved": cell_tf, "peak": fp64_peak,
                      "unit": "TFLOP/s", "frac": cell_tf / fp64_peak, "traffic": None,
                      "peak_source": "measured live: DFMA-chain kernel on this GPU",
                      "algorithmic_flops_per_launch": FP64_OPS_PER_CELL_SOLVE * n,
                      "per_unit": f"{FP64_OPS_PER_CELL_SOLVE:.0f} FP64 flops per cell solve "
-                                 "(ncu instruction counts, profiles/cell_kernel_slab96.md)"},
+                                 "(ncu instruction counts, profiles/cell_kernels_slab96.md)"},
         "roofline_hbm": {"kernel": "ss_columns_kernel (3 axis passes, one outer iteration)",
                          "bound": "hbm", "achieved": col_gbs, "peak": hbm, "unit": "GB/s",
                          "frac": col_gbs / hbm, "traffic": None, "peak_source": peak_kind,
@@ -227,13 +228,70 @@ def run_gb300(args, ws, rank, local):
         "clocks": clk.summary(),
     }
     out["cpu_baseline"] = cpu_baseline(args, dens, g0, nside, zeta, cell, float(np.mean(iters)))
+    if args.network_cells > 0:
+        out["network"] = network_bench(args)
     return out
 
 
-# FP64 flops (DFMA = 2, DADD/DMUL = 1) per cell solve of the mixed cell
-# kernel on the 14th outer iteration of the 96^3 slab, every cell active, from
-# the ncu instruction counts in profiles/cell_kernel_slab96.md.
-FP64_OPS_PER_CELL_SOLVE = 5330.0
+def network_bench(args):
+    """Full 31-species network steady state (the reference's per-cell BDF
+    solve, prism3d/chemistry/solver.py:145-225) on seeded cells: device time
+    of the mixed and FP64 kernels, the host-buffer C ABI end to end, and the
+    CPU oracle on a bounded sample."""
+    import numpy as np
+    import torch
+
+    from prism3d_gb300 import fields
+    from prism3d_gb300.network import ChemistrySolverGPU
+
+    n = args.network_cells
+    net = ChemistrySolverGPU()
+    cond = fields.network_cells(n, seed=11)
+    x0 = net.default_initial_batch(cond[:, 2], cond[:, 3])
+    dc = torch.from_numpy(cond).cuda()
+    dx0 = torch.from_numpy(x0).cuda()
+    res = {"cells": n, "workload": "seeded cells over the PDR parameter span "
+           "(prism3d_gb300/fields.py:network_cells), the reference's initial abundances",
+           "rtol": 1e-8, "max_iter": 300}
+    for mixed in (True, False):
+        for rep in range(2):  # one warm-up, one timed
+            dx = dx0.clone()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            st, it = net.solve_steady_state_batch(dc, dx, mixed=mixed, post=True,
+                                                  return_iters=True)
+            e1.record()
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        st, it = st.cpu().numpy(), it.cpu().numpy()
+        res["mixed" if mixed else "fp64"] = {
+            "value": n / (ms * 1e-3), "unit": "cells/s", "ms": ms,
+            "newton_iters_mean": float(it.mean()), "unconverged_frac": float((st != 0).mean())}
+    t0 = time.perf_counter()
+    xh = x0.copy()
+    net.solve_steady_state_batch(cond, xh, mixed=True, post=True)
+    t = time.perf_counter() - t0
+    res["e2e"] = {"value": n / t, "unit": "cells/s", "h2d_bytes": int(cond.nbytes + x0.nbytes),
+                  "d2h_bytes": int(x0.nbytes + 8 * n)}
+    net.close()
+    # CPU oracle (NumPy restatement of the same method, vectorised over cells)
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from oracle import network as ON
+    m = min(args.network_cpu_sample, n)
+    t0 = time.perf_counter()
+    ON.solve_steady_state(ON.load(), x0[:m], cond[:m])
+    t = time.perf_counter() - t0
+    res["cpu_baseline"] = {"value": m / t, "unit": "cells/s", "cores": 1, "kind": "port",
+                           "sample": f"first {m} cells, NumPy oracle"}
+    return res
+
+
+# FP64 flops (DFMA = 2, DADD/DMUL = 1) per cell solve of the mixed chemistry
+# and thermal kernels on the 14th outer iteration of the 96^3 slab, every
+# cell active, from the ncu instruction counts in
+# profiles/cell_kernels_slab96.md (1,754 + 3,425).
+FP64_OPS_PER_CELL_SOLVE = 5179.0
 
 
 def fp64_peak_tflops():
@@ -317,6 +375,9 @@ def main():
     ap.add_argument("--plain-full", action="store_true")
     ap.add_argument("--plain-iters", type=int, default=20)
     ap.add_argument("--ref-iters", type=int, default=700)
+    ap.add_argument("--network-cells", type=int, default=1 << 20,
+                    help="cells of the full-network measurement (0: skip)")
+    ap.add_argument("--network-cpu-sample", type=int, default=2048)
     args = ap.parse_args()
     ws, rank, local = _dist()
     if ws > 1:

@@ -255,6 +255,9 @@ int p3d_steady_run(p3d_steady_t *s, int mixed, int64_t max_outer, double tol, in
                    double w_chem, double w_t, int64_t *iters_out, double *dmax_out);
 int p3d_steady_get(p3d_steady_t *s, int field, double *host_out);
 int p3d_steady_get_ray(p3d_steady_t *s, int32_t *host_out);
+/* Overwrite one state field (P3D_F_T_GAS or P3D_F_X_HI..P3D_F_X_CO) from
+ * host memory, e.g. after p3d_steady_reset; values must be finite and > 0. */
+int p3d_steady_set(p3d_steady_t *s, int field, const double *host_in);
 /* 9 doubles per iteration: largest relative change, chemistry and thermal
  * failures, cells changing more than 100 tol / tol / tol / 100, FP64
  * net-heating evaluations, grid-mean T, cells solved. */
@@ -267,6 +270,33 @@ int p3d_steady_elapsed_ms(p3d_steady_t *s, double *ms);
  * chain kernel timed with CUDA events): the peak the per-cell kernels, which
  * are bound by the FP64 pipe, are reported against. */
 int p3d_fp64_peak_tflops(double *tflops);
+/* Multipliers (> 0) of the reduced network's eight rate coefficients in the
+ * steady-state solve, in this order: H2 formation, H2 photodissociation, H2
+ * cosmic-ray destruction, C photoionisation, C+ recombination, CO
+ * photodissociation, CR-induced CO dissociation, C + OH -> CO
+ * (solver_3d.py:549-557, chemistry.rs:35-49).  1 = the reference's rates.
+ * Takes effect at the next p3d_steady_run. */
+int p3d_steady_set_rate_scale(p3d_steady_t *s, const double *scale8);
+/* 1: hold T_gas at its current values in later p3d_steady_run calls (no
+ * thermal balance; chemistry and shielding only), 0: solve it (default). */
+int p3d_steady_set_fixed_temperature(p3d_steady_t *s, int fixed);
+/* Adjoint of the converged steady state (implicit-function theorem): the
+ * gradient of L = sum_cells n_H dx (w6[0] x_HI + w6[1] x_H2 + w6[2] x_C+ +
+ * w6[3] x_C + w6[4] x_CO) + w6[5] mean(T_gas) -- weighted column sums over
+ * the grid and the mean temperature -- with respect to the log multipliers
+ * of the eight rate coefficients above and log G0 (grad9[8]).  Transposed
+ * per-cell 6x6 solves (chemistry rows and thermal balance) and reverse
+ * scans of the selected-ray H2/CO columns plus the grid-mean T coupling, as
+ * block-Jacobi sweeps relaxed by omega (0, 1], until the gradient changes by
+ * <= tol relative to its largest component between checks 20 sweeps apart
+ * (at most max_sweeps sweeps).  dx is the cell size [cm].  loss2
+ * (optional): the column term and mean(T_gas); n_jump_out: cells whose T is
+ * held (on a jump of the net heating, at a bracket end, or all with a fixed
+ * temperature).  P3D_ECONVERGE if tol was not reached.  No counterpart in
+ * the reference. */
+int p3d_steady_adjoint(p3d_steady_t *s, const double *w6, double dx, int64_t max_sweeps,
+                       double tol, double omega, double *grad9, double *loss2,
+                       int64_t *sweeps_out, int64_t *n_jump_out);
 /* Kernels launched on the device since the last p3d_steady_reset. */
 int p3d_steady_launch_count(p3d_steady_t *s, int64_t *out);
 /* Mean time (ms) over reps launches on the current state of: the three

@@ -49,12 +49,16 @@ SIGNATURES = {
     "p3d_steady_run": [_vp, ctypes.c_int, _i64, _f64, _i64, _f64, _f64, _I64, _D],
     "p3d_steady_get": [_vp, ctypes.c_int, _D],
     "p3d_steady_get_ray": [_vp, _I32],
+    "p3d_steady_set": [_vp, ctypes.c_int, _D],
     "p3d_steady_history": [_vp, _D, _i64, _I64],
     "p3d_steady_destroy": [_vp],
     "p3d_steady_launch_count": [_vp, _I64],
     "p3d_steady_elapsed_ms": [_vp, _D],
     "p3d_fp64_peak_tflops": [_D],
     "p3d_steady_kernel_times": [_vp, ctypes.c_int, _D],
+    "p3d_steady_set_rate_scale": [_vp, _D],
+    "p3d_steady_set_fixed_temperature": [_vp, ctypes.c_int],
+    "p3d_steady_adjoint": [_vp, _D, _f64, _i64, _f64, _f64, _D, _D, _I64, _I64],
     "p3d_network_create": [ctypes.POINTER(_vp), _i32, _i32, _I32, _D, _D, _D, _I32, _I32, _I32,
                            _i32, _D, _I32, _i32, _f64, _i32, _f64, _f64],
     "p3d_network_rhs": [_vp, _i64, _D, _D, _D],

@@ -36,6 +36,7 @@ struct ChemCell {
   double n_h, kci, acp, rh2, rcr, xc, hcop;
   double kpd0, kco0, kco_cr, u_h2, u_co, ds, b_dop;
   double fh2_fix, kpd_fix, kco_fix;  // used when ds == 0 (see chem_prepare)
+  double koh_s = 1.0;                // multiplier of the C + OH -> CO rate
 };
 
 // Shielding factors and the photo rates they set, once per cell when the
@@ -54,7 +55,7 @@ __device__ __forceinline__ void chem5_eval(const ChemCell& p, const double* y, d
   double s = 10.0 * h;
   double x_oh = 1e-9 + 9e-8 * fmin(fmax(s, 0.0), 1.0);
   double dxoh = (s > 0.0 && s < 1.0) ? 9e-7 : 0.0;
-  double koh = 1e-10 * x_oh * p.n_h;
+  double koh = 1e-10 * p.koh_s * x_oh * p.n_h;
   double an = p.acp * p.n_h;
   double xe = cp + p.hcop;
   double f1, kpd, kco, dkpd_h = 0.0, dkco_h = 0.0;
@@ -90,7 +91,7 @@ __device__ __forceinline__ void chem5_eval(const ChemCell& p, const double* y, d
   J[2][2] = -an * (xe + cp);
   J[2][3] = p.kci;
   J[2][4] = kco;
-  J[3][1] = 1e-10 * dxoh * p.n_h * c - co * dkco_h;
+  J[3][1] = 1e-10 * p.koh_s * dxoh * p.n_h * c - co * dkco_h;
   J[3][3] = koh;
   J[3][4] = -kco;
   J[4][2] = 1.0;

@@ -16,6 +16,7 @@
 #include "p3d_rt.cuh"
 #include "p3d_steady.cuh"
 #include "p3d_steady_kernels.cuh"
+#include "p3d_adjoint.cuh"
 
 namespace p3d {
 
@@ -147,6 +148,8 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   p.therm_tol_mixed = 1e-10;
   p.chem_max_iter = 200; p.therm_max_iter = 80; p.n_rays = (int)n_rays;
   p.h2_implicit = 0;
+  for (int k = 0; k < 8; ++k) p.rs[k] = 1.0;
+  p.fix_t = 0;
   p.pe = PeGrid{log_psi_min, log_psi_step, eg_min, eg_step, (int)n_psi, (int)n_eg};
   memcpy(p.lines.cii, cii, sizeof(p.lines.cii));
   memcpy(p.lines.oi63, oi63, sizeof(p.lines.oi63));
@@ -412,6 +415,30 @@ int p3d_steady_get(p3d_steady_t* h, int field, double* host_out) {
   return e == cudaSuccess ? P3D_OK : cuda_fail(e, "steady get");
 }
 
+int p3d_steady_set(p3d_steady_t* h, int field, const double* host_in) {
+  if (!h || !host_in) return set_error(P3D_EINVAL, "null argument");
+  SteadySolver* s = &h->s;
+  SteadyDev& d = s->d;
+  double* dst = nullptr;
+  switch (field) {
+    case P3D_F_T_GAS: dst = d.t_gas; break;
+    case P3D_F_X_HI: dst = d.x_hi; break;
+    case P3D_F_X_H2: dst = d.x_h2; break;
+    case P3D_F_X_CP: dst = d.x_cp; break;
+    case P3D_F_X_C: dst = d.x_c; break;
+    case P3D_F_X_CO: dst = d.x_co; break;
+    default: return set_error(P3D_EINVAL, "field %d cannot be set (T_gas and the five "
+                              "chemistry unknowns can)", field);
+  }
+  for (int64_t i = 0; i < s->n; ++i)
+    if (!(host_in[i] > 0.0) || !std::isfinite(host_in[i]))
+      return set_error(P3D_EINVAL, "value %lld must be finite and > 0", (long long)i);
+  cudaError_t e = cudaMemcpyAsync(dst, host_in, sizeof(double) * s->n, cudaMemcpyHostToDevice,
+                                  s->st->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->st->stream);
+  return e == cudaSuccess ? P3D_OK : cuda_fail(e, "steady set");
+}
+
 int p3d_steady_get_ray(p3d_steady_t* h, int32_t* host_out) {
   if (!h || !host_out) return set_error(P3D_EINVAL, "null argument");
   SteadySolver* s = &h->s;
@@ -532,6 +559,170 @@ int p3d_fp64_peak_tflops(double* tflops) {
   cudaEventDestroy(e1);
   if (e != cudaSuccess) return cuda_fail(e, "fp64 peak probe");
   *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
+  return P3D_OK;
+}
+
+int p3d_steady_set_rate_scale(p3d_steady_t* h, const double* scale8) {
+  if (!h || !scale8) return set_error(P3D_EINVAL, "null argument");
+  for (int k = 0; k < 8; ++k)
+    if (!(scale8[k] > 0.0) || !std::isfinite(scale8[k]))
+      return set_error(P3D_EINVAL, "rate scale %d must be finite and > 0", k);
+  for (int k = 0; k < 8; ++k) h->s.par.rs[k] = scale8[k];
+  return P3D_OK;
+}
+
+int p3d_steady_set_fixed_temperature(p3d_steady_t* h, int fixed) {
+  if (!h) return set_error(P3D_EINVAL, "null handle");
+  h->s.par.fix_t = fixed ? 1 : 0;
+  return P3D_OK;
+}
+
+int p3d_steady_adjoint(p3d_steady_t* h, const double* w6, double dx, int64_t max_sweeps,
+                       double tol, double omega, double* grad9, double* loss2,
+                       int64_t* sweeps_out, int64_t* n_jump_out) {
+  if (!h || !grad9 || !w6) return set_error(P3D_EINVAL, "null argument");
+  if (max_sweeps < 1 || !(tol > 0.0) || !(dx > 0.0) || !(omega > 0.0 && omega <= 1.0))
+    return set_error(P3D_EINVAL, "max_sweeps >= 1, tol > 0, dx > 0, 0 < omega <= 1 required");
+  SteadySolver* s = &h->s;
+  if (s->iters_done < 1) return set_error(P3D_EINVAL, "run the steady state before its adjoint");
+  cudaStream_t str = s->st->stream;
+  const int64_t n = s->n;
+  const SteadyDev& d = s->d;
+  // workspace (freed on return)
+  std::vector<void*> mem;
+  auto get = [&](size_t bytes) -> void* {
+    void* q = nullptr;
+    if (cudaMalloc(&q, bytes ? bytes : 8) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    mem.push_back(q);
+    return q;
+  };
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(str);
+    for (void* q : mem) cudaFree(q);
+  };
+  AdjArgs a;
+  for (int k = 0; k < 6; ++k) a.w[k] = w6[k];
+  const size_t nd = sizeof(double) * (size_t)n;
+  a.jinv = (double*)get(36 * nd);
+  a.jn2 = (double*)get(6 * nd);
+  a.jn3 = (double*)get(6 * nd);
+  a.jb = (double*)get(6 * nd);
+  a.jth = (double*)get(6 * kAdjParams * nd);
+  a.lam = (double*)get(6 * nd);
+  a.cx2 = (double*)get(nd);
+  a.cx3 = (double*)get(nd);
+  a.a2 = (double*)get(nd);
+  a.a3 = (double*)get(nd);
+  a.qb = (double*)get(nd);
+  a.jump = (int*)get(sizeof(int) * (size_t)n);
+  a.red = (double*)get(sizeof(double) * (size_t)s->nparts);
+  a.scal = (double*)get(sizeof(double) * 2);
+  a.dmax = (unsigned long long*)get(sizeof(unsigned long long));
+  unsigned int* n_bad = (unsigned int*)get(sizeof(unsigned int));
+  for (void* q : mem)
+    if (!q) {
+      cleanup();
+      return set_error(P3D_ENOMEM, "adjoint workspace (%lld cells)", (long long)n);
+    }
+  // columns and mean T of the final state
+  const SteadyParams& par = s->par;
+  int64_t dims[3] = {s->nx, s->ny, s->nz};
+  for (int axis = 0; axis < 3; ++axis) {
+    int64_t np = n / dims[axis];
+    ss_columns_kernel<<<(unsigned)ceil_div(np, 128), 128, 0, str>>>(
+        axis, par.h2_implicit, s->nx, s->ny, s->nz, np, s->dens, d.x_h2, d.x_co, d.fam, d.ds,
+        d.u_h2, d.u_co);
+  }
+  ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(n, d.t_gas, s->parts);
+  ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, n, s->glob);
+  SteadyGlobals gl;
+  cudaError_t e = cudaMemcpyAsync(&gl, s->glob, sizeof(gl), cudaMemcpyDeviceToHost, str);
+  if (e == cudaSuccess) e = cudaMemsetAsync(n_bad, 0, sizeof(unsigned int), str);
+  if (e == cudaSuccess) e = cudaMemsetAsync(a.lam, 0, 6 * nd, str);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+  if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "adjoint setup"); }
+  const double b = gl.b_dop, dbdt = gl.b_dop / (2.0 * gl.t_mean);
+  const unsigned grid = grid_for(n, s->st->sms, 4);
+  adj_local_kernel<<<(unsigned)ceil_div(n, 128) < grid * 2u ? (unsigned)ceil_div(n, 128)
+                                                             : grid * 2u,
+                     128, 0, str>>>(n, d, par, s->a_nano, s->a_rest, b, a, n_bad);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "adjoint local launch"); }
+  auto grid_sum = [&](const double* q, double* out) {
+    ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(n, q, a.red);
+    adj_finish_sum_kernel<<<1, 32, 0, str>>>(s->nparts, a.red, out);
+  };
+  // sweeps until the gradient changes by <= tol (relative to its largest
+  // component) between checks
+  auto gradient = [&](double* out) -> cudaError_t {
+    for (int k = 0; k < kAdjParams; ++k) {
+      adj_grad_kernel<<<grid, kThreads, 0, str>>>(n, a, k, a.cx2);
+      grid_sum(a.cx2, a.scal + 1);
+      cudaError_t e2 = cudaMemcpyAsync(out + k, a.scal + 1, sizeof(double),
+                                       cudaMemcpyDeviceToHost, str);
+      if (e2 != cudaSuccess) return e2;
+    }
+    return cudaStreamSynchronize(str);
+  };
+  int64_t sweeps = 0;
+  double dmax = INFINITY;
+  double prev[kAdjParams];
+  for (int k = 0; k < kAdjParams; ++k) prev[k] = 0.0;
+  const int kCheck = 20;
+  while (sweeps < max_sweeps) {
+    for (int k = 0; k < kCheck && sweeps < max_sweeps; ++k, ++sweeps) {
+      adj_couple_kernel<<<grid, kThreads, 0, str>>>(n, d, a);
+      for (int axis = 0; axis < 3; ++axis) {
+        int64_t np = n / dims[axis];
+        adj_scan_kernel<<<(unsigned)ceil_div(np, 128), 128, 0, str>>>(
+            axis, s->nx, s->ny, s->nz, np, s->dens, d.fam, a);
+      }
+      grid_sum(a.qb, a.scal);
+      cudaMemsetAsync(a.dmax, 0, sizeof(unsigned long long), str);
+      adj_update_kernel<<<grid, kThreads, 0, str>>>(n, d, a, dx, a.scal, dbdt, omega);
+    }
+    e = gradient(grad9);
+    if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "adjoint sweeps"); }
+    double gm = 0.0, dg = 0.0;
+    for (int k = 0; k < kAdjParams; ++k) {
+      gm = fmax(gm, fabs(grad9[k]));
+      dg = fmax(dg, fabs(grad9[k] - prev[k]));
+      prev[k] = grad9[k];
+    }
+    dmax = gm > 0.0 ? dg / gm : dg;
+    if (!std::isfinite(dmax)) break;
+    if (dmax <= tol) break;
+  }
+  double lc = 0.0, lt = 0.0;
+  adj_loss_kernel<<<grid, kThreads, 0, str>>>(n, d, a, dx, a.cx2, a.cx3);
+  grid_sum(a.cx2, a.scal + 1);
+  e = cudaMemcpyAsync(&lc, a.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, str);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+  grid_sum(a.cx3, a.scal + 1);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&lt, a.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, str);
+  // jump cells
+  adj_jump_count_kernel<<<grid, kThreads, 0, str>>>(n, a.jump, a.cx2);
+  grid_sum(a.cx2, a.scal + 1);
+  double nj = 0.0;
+  unsigned int bad = 0;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&nj, a.scal + 1, sizeof(double), cudaMemcpyDeviceToHost, str);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&bad, n_bad, sizeof(bad), cudaMemcpyDeviceToHost, str);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+  cleanup();
+  if (e != cudaSuccess) return cuda_fail(e, "adjoint results");
+  if (loss2) { loss2[0] = lc; loss2[1] = lt / (double)n; }
+  if (sweeps_out) *sweeps_out = sweeps;
+  if (n_jump_out) *n_jump_out = (int64_t)nj;
+  if (bad) return set_error(P3D_ECONVERGE, "adjoint: %u cells with a singular Jacobian", bad);
+  if (!(dmax <= tol))
+    return set_error(P3D_ECONVERGE, "adjoint sweeps did not reach tol (last relative gradient "
+                     "change %.3e after %lld sweeps)", dmax, (long long)sweeps);
   return P3D_OK;
 }
 

@@ -45,6 +45,12 @@ struct SteadyParams {
   double count_thr[3];  // thresholds of the n_gt counters
   double quiet_tol;     // mixed path: skip cells whose last change was <= this
   double quiet_in_tol;  // ... and whose inputs moved <= this since
+  // multipliers of the reduced network's rate coefficients (1 = the
+  // reference's): H2 formation, H2 photodissociation, H2 cosmic-ray
+  // destruction, C photoionisation, C+ recombination, CO photodissociation,
+  // CR-induced CO dissociation, C + OH -> CO
+  double rs[8];
+  int fix_t;  // 1: T_gas is held at its current value (no thermal balance)
   PeGrid pe;
   LineParams lines;
 };

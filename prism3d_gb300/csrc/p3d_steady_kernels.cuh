@@ -300,15 +300,16 @@ ss_chem_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g,
     // chemistry (solver_3d.py:549-557 rates; steady state of chemistry.rs:35-49)
     ChemCell cc;
     cc.n_h = nh;
-    cc.kci = d.kci[i];
-    cc.acp = 4.67e-12 * pow(tg / 300.0, -0.6);
-    cc.rh2 = rh2 * nh * 0.5;
-    cc.rcr = 2.5 * zeta * 0.1;
+    cc.kci = d.kci[i] * p.rs[3];
+    cc.acp = 4.67e-12 * pow(tg / 300.0, -0.6) * p.rs[4];
+    cc.rh2 = rh2 * nh * 0.5 * p.rs[0];
+    cc.rcr = 2.5 * zeta * 0.1 * p.rs[2];
     cc.xc = p.x_c_total;
     cc.hcop = p.x_hcop;
-    cc.kpd0 = d.kpd0[i];
-    cc.kco0 = d.kco0[i];
-    cc.kco_cr = 6.0 * zeta;
+    cc.kpd0 = d.kpd0[i] * p.rs[1];
+    cc.kco0 = d.kco0[i] * p.rs[5];
+    cc.kco_cr = 6.0 * zeta * p.rs[6];
+    cc.koh_s = p.rs[7];
     cc.u_h2 = d.u_h2[i];
     cc.u_co = d.u_co[i];
     cc.ds = p.h2_implicit ? d.ds[i] : 0.0;
@@ -385,11 +386,12 @@ ss_thermal_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
     c.n_o_nh = d.x_o[i] * nh;
     c.n_c_nh = x3 * nh;
     int tst = 0, nev = 0;
-    double troot = MIXED ? root_mixed(c, p.lines, c_co_ss, p.theta2, c_lines32, c_co32,
-                                      g_bisect_mid, p.therm_tol_mixed, p.therm_max_iter,
-                                      d.t_root[i], &tst, &nev)
-                         : root_plain(c, p.lines, c_co_ss, p.theta2, p.therm_tol,
-                                      p.therm_max_iter, &tst, &nev);
+    double troot = p.fix_t ? tg
+                   : MIXED ? root_mixed(c, p.lines, c_co_ss, p.theta2, c_lines32, c_co32,
+                                        g_bisect_mid, p.therm_tol_mixed, p.therm_max_iter,
+                                        d.t_root[i], &tst, &nev)
+                           : root_plain(c, p.lines, c_co_ss, p.theta2, p.therm_tol,
+                                        p.therm_max_iter, &tst, &nev);
     my_evals += (unsigned long long)nev;
     my_fail += (unsigned)tst;
     double tp = d.t_prev[i], rp = d.r_prev[i], lo = d.t_lo[i], hi = d.t_hi[i], sp = d.span[i];

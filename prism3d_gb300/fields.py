@@ -83,6 +83,18 @@ WORKLOADS = {
 }
 
 
+def network_cells(n, seed=1):
+    """Per-cell conditions (n, 7: n_H, T, G0, A_V, zeta, f_sh_H2, f_sh_CO) for
+    the full-network benchmark: log-uniform n_H 10-3e6 cm^-3, T 10-1e4 K, G0
+    0.1-1e5, uniform A_V 0-20, zeta 1e-17-1e-15 s^-1, f_sh_H2 1e-8-1,
+    f_sh_CO 1e-6-1 (the span of the PDR cells the network is solved on)."""
+    rng = np.random.default_rng(seed)
+    return np.ascontiguousarray(np.stack(
+        [10 ** rng.uniform(1, 6.5, n), 10 ** rng.uniform(1, 4, n), 10 ** rng.uniform(-1, 5, n),
+         rng.uniform(0, 20, n), 10 ** rng.uniform(-17, -15, n), 10 ** rng.uniform(-8, 0, n),
+         10 ** rng.uniform(-6, 0, n)], axis=1))
+
+
 def workload(name, seed=1):
     """(density, G0_rays (per-ray array, source on -x), nside, zeta0, cell_size)."""
     from .core import directional_G0

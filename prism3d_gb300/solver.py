@@ -96,6 +96,55 @@ class PDRSolverGPU:
         L.check("p3d_steady_run", rc)
         return True
 
+    RATE_NAMES = ("H2_formation", "H2_photodiss", "H2_cr_destruction", "C_photoion",
+                  "Cp_recombination", "CO_photodiss", "CO_cr_dissociation", "C_OH_to_CO")
+
+    def set_rate_scale(self, scale):
+        """Multipliers of the reduced network's eight rate coefficients
+        (RATE_NAMES order; 1 = the reference's), used from the next run()."""
+        sc = np.ascontiguousarray(scale, dtype=np.float64)
+        if sc.shape != (8,):
+            raise ValueError("rate scale needs 8 values")
+        L.call("p3d_steady_set_rate_scale", self._h, L.dptr(sc))
+
+    def set_fixed_temperature(self, fixed=True):
+        """Hold T_gas at its current values in later run() calls (chemistry
+        and shielding only) or solve the thermal balance again."""
+        L.call("p3d_steady_set_fixed_temperature", self._h, int(bool(fixed)))
+
+    def adjoint(self, w_columns=(0.0, 0.0, 1.0, 1.0, 1.0), w_T=1.0, max_sweeps=20000, tol=1e-10,
+                omega=0.5):
+        """Gradient of L = sum_cells n_H dx sum_s w_columns[s] x_s + w_T mean(T_gas)
+        (s = x_HI, x_H2, x_C+, x_C, x_CO: weighted column sums over the grid)
+        at the converged state with respect to the log rate multipliers
+        (RATE_NAMES) and log G0.  Returns a dict with 'grad' (9,), 'loss_col',
+        'loss_T', 'sweeps', 'n_jump', 'converged' (sweeps reached tol) and
+        'message'."""
+        w = np.zeros(6)
+        w[:5] = np.asarray(w_columns, float)
+        w[5] = float(w_T)
+        g = np.zeros(9)
+        loss = np.zeros(2)
+        sw = L._i64(0)
+        nj = L._i64(0)
+        rc = L.lib.p3d_steady_adjoint(self._h, L.dptr(w), self.cell_size, int(max_sweeps),
+                                      float(tol), float(omega), L.dptr(g), L.dptr(loss),
+                                      ctypes.byref(sw), ctypes.byref(nj))
+        if rc != -5:  # P3D_ECONVERGE: tol not reached, results kept
+            L.check("p3d_steady_adjoint", rc)
+        return {"grad": g, "loss_col": float(loss[0]), "loss_T": float(loss[1]),
+                "sweeps": int(sw.value), "n_jump": int(nj.value), "converged": rc == 0,
+                "message": "" if rc == 0 else L.lib.p3d_last_error().decode()}
+
+    def set(self, name, values):
+        """Overwrite T_gas or one of x_HI, x_H2, x_Cp, x_C, x_CO on the device."""
+        v = np.ascontiguousarray(values, dtype=np.float64).reshape(-1)
+        if v.size != self.n_cells:
+            raise ValueError(f"{name}: {v.size} values for {self.n_cells} cells")
+        if name not in ("T_gas", "x_HI", "x_H2", "x_Cp", "x_C", "x_CO"):
+            raise KeyError(name)
+        L.call("p3d_steady_set", self._h, FIELDS[name], L.dptr(v))
+
     def get(self, name):
         out = np.empty(self.n_cells)
         L.call("p3d_steady_get", self._h, FIELDS[name], L.dptr(out))

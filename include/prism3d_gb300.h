@@ -289,14 +289,18 @@ int p3d_steady_set_fixed_temperature(p3d_steady_t *s, int fixed);
  * scans of the selected-ray H2/CO columns plus the grid-mean T coupling, as
  * block-Jacobi sweeps relaxed by omega (0, 1], until the gradient changes by
  * <= tol relative to its largest component between checks 20 sweeps apart
- * (at most max_sweeps sweeps).  dx is the cell size [cm].  loss2
+ * (at most max_sweeps sweeps).  dx is the cell size [cm].  grad_ln_nh
+ * (optional, n_cells host doubles): the gradient with respect to each cell's
+ * log n_H -- its own residual, its layers in the selected-ray H2/CO columns
+ * of the cells downstream, and the ray march (G0 over every ray carrying
+ * external field, A_V and N_H over the selected ray, whose choice is held).  loss2
  * (optional): the column term and mean(T_gas); n_jump_out: cells whose T is
  * held (on a jump of the net heating, at a bracket end, or all with a fixed
  * temperature).  P3D_ECONVERGE if tol was not reached.  No counterpart in
  * the reference. */
 int p3d_steady_adjoint(p3d_steady_t *s, const double *w6, double dx, int64_t max_sweeps,
-                       double tol, double omega, double *grad9, double *loss2,
-                       int64_t *sweeps_out, int64_t *n_jump_out);
+                       double tol, double omega, double *grad9, double *grad_ln_nh,
+                       double *loss2, int64_t *sweeps_out, int64_t *n_jump_out);
 /* Kernels launched on the device since the last p3d_steady_reset. */
 int p3d_steady_launch_count(p3d_steady_t *s, int64_t *out);
 /* Mean time (ms) over reps launches on the current state of: the three

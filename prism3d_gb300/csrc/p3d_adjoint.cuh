@@ -47,6 +47,8 @@ struct AdjArgs {
   double* a3;     // n: ds dG/dN_CO . lam
   double* qb;     // n: dG/db . lam
   int* jump;      // n
+  double* teval;  // n: thermal-row evaluation point (<= 0: T itself)
+  double* dn;     // n: gradient with respect to log n_H
   double* red;    // reduction scratch (one value per block of the sums)
   double* scal;   // 2: qb total, a sum result
   unsigned long long* dmax;  // largest relative change of lam in the last sweep (bits)
@@ -56,31 +58,50 @@ struct AdjArgs {
 // Per-cell residual G (6) at state u (6), columns n2, n3, Doppler b and log
 // parameter offsets th (kAdjParams) -- the equations the forward kernels
 // zero at the fixed point.
+// Density-dependent inputs of a cell's residual: its own n_H and the ray-march
+// results G0, A_V and N_H (selected ray) the per-cell constants derive from
+// (ss_setup_kernel).
+struct AdjStatic {
+  double nh, g0, av, nhc;
+};
+
+__device__ __forceinline__ AdjStatic adj_static(const SteadyDev& d, int64_t i) {
+  return AdjStatic{d.dens[i], d.g0[i], d.av[i], d.nh_col[i]};
+}
+
 __device__ void adj_residual(int64_t i, const SteadyDev& d, const SteadyParams& p,
                              const double* __restrict__ a_nano, const double* __restrict__ a_rest,
                              const double* u, double n2, double n3, double b, const double* th,
-                             double t_eval, double* G) {
-  const double nh = d.dens[i];
+                             double t_eval, const AdjStatic& st, double* G) {
+  const double nh = st.nh;
   const double T = u[5];
   const double gs = exp(th[8]);
   double m[8];
 #pragma unroll
   for (int k = 0; k < 8; ++k) m[k] = p.rs[k] * exp(th[k]);
-  const double g0 = d.g0[i] * gs, av = d.av[i];
+  const double av = st.av;
+  const double g0 = st.g0 * gs;
+  // per-cell constants as ss_setup_kernel forms them
+  const double e374 = exp(-3.74 * av);
+  const double kpd0 = 4.43e-11 * g0 * e374;
+  const double uv0 = g0 * e374;
+  const double kci = 2.56e-10 * g0 * exp(-3.02 * av);
+  const double kco0 = 1.71e-10 * g0 * exp(-3.53 * av);
+  const double hci0 = 3.0e-10 * g0 * exp(-3.0 * av);
+  const double zeta = cr_rate(st.nhc, p.zeta0);
   const double xe = fmax(u[2] + p.x_hcop, 1e-30);
   const double td = tdust(tdust_rad(g0, av), nh, T);
   const double rh2 = h2_form(T, td, p.f_nano, p.sigma_nano, p.sigma_lc, p.sigma_sil);
-  const double zeta = d.zeta[i];
   ChemCell cc;
   cc.n_h = nh;
-  cc.kci = d.kci[i] * gs * m[3];
+  cc.kci = kci * m[3];
   cc.acp = 4.67e-12 * pow(T / 300.0, -0.6) * m[4];
   cc.rh2 = rh2 * nh * 0.5 * m[0];
   cc.rcr = 2.5 * zeta * 0.1 * m[2];
   cc.xc = p.x_c_total;
   cc.hcop = p.x_hcop;
-  cc.kpd0 = d.kpd0[i] * gs * m[1];
-  cc.kco0 = d.kco0[i] * gs * m[5];
+  cc.kpd0 = kpd0 * m[1];
+  cc.kco0 = kco0 * m[5];
   cc.kco_cr = 6.0 * zeta * m[6];
   cc.koh_s = m[7];
   cc.u_h2 = n2;
@@ -94,13 +115,13 @@ __device__ void adj_residual(int64_t i, const SteadyDev& d, const SteadyParams& 
   for (int k = 0; k < 5; ++k) G[k] = f[k];
   const double x0 = u[0], x1 = u[1], x3 = u[3];
   ThermalCtx c;
-  const double uv = d.uv0[i] * gs * fh2;
+  const double uv = uv0 * fh2;
   double gf = pe_cell(p.pe, a_nano, a_rest, g0, T, xe, nh, p.f_nano, p.e_g);
   gf += 3.3e-11 * uv * x1 * nh * (0.4 * kEVtoErg);
   gf += rh2 * x0 * (nh * nh) * (1.5 * kEVtoErg);
   gf += 3.0e-10 * uv * x1 * nh * (2.0 * kEVtoErg) * (nh / (nh + 3e4));
   gf += zeta * (x0 + 2.0 * x1) * nh * (20.0 * kEVtoErg);
-  gf += d.hci0[i] * gs * x3 * nh * kEVtoErg;
+  gf += hci0 * x3 * nh * kEVtoErg;
   c.gamma_fixed = gf;
   const double mu = x1 > 0.5 ? 2.0 : 1.0;
   c.gg_coeff = 2.0 * 0.35 * 1e-21 * (nh * nh) * sqrt(8.0 * kKBoltz / (kPi * mu * kMH)) * kKBoltz;
@@ -154,11 +175,12 @@ adj_local_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restric
        i += (int64_t)gridDim.x * blockDim.x) {
     double u[6] = {d.x_hi[i], d.x_h2[i], d.x_cp[i], d.x_c[i], d.x_co[i], d.t_gas[i]};
     const double n2 = d.u_h2[i], n3 = d.u_co[i];
+    const AdjStatic st = adj_static(d, i);
     double th[kAdjParams];
 #pragma unroll
     for (int k = 0; k < kAdjParams; ++k) th[k] = 0.0;
     double G0[6], Gp[6], Gm[6];
-    adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b, th, -1.0, G0);
+    adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b, th, -1.0, st, G0);
     // Thermal row.  A smooth root: net_heating(T) = 0.  Otherwise the outer
     // map T -> selected root is discontinuous at T: either the net heating
     // itself jumps there (T held: dT = 0), or one of the ten bisection
@@ -173,14 +195,14 @@ adj_local_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restric
       for (int q = 0; q < 6; ++q) { up[q] = u[q]; um[q] = u[q]; }
       up[5] += hT;
       um[5] -= hT;
-      adj_residual(i, d, p, a_nano, a_rest, up, n2, n3, b, th, -1.0, Gp);
-      adj_residual(i, d, p, a_nano, a_rest, um, n2, n3, b, th, -1.0, Gm);
+      adj_residual(i, d, p, a_nano, a_rest, up, n2, n3, b, th, -1.0, st, Gp);
+      adj_residual(i, d, p, a_nano, a_rest, um, n2, n3, b, th, -1.0, st, Gm);
       if (!(fabs(G0[5]) <= 0.05 * fabs(Gp[5] - Gm[5]))) {
         double lo = 10.0, hi = 1e5, best = INFINITY, t_best = -1.0, nmax = 0.0;
         double nk[10], tk[10];
         for (int k = 0; k < 10; ++k) {
           const double tm = sqrt(lo * hi);
-          adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b, th, tm, Gp);
+          adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b, th, tm, st, Gp);
           nk[k] = Gp[5];
           tk[k] = tm;
           nmax = fmax(nmax, fabs(Gp[5]));
@@ -199,37 +221,37 @@ adj_local_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restric
       for (int q = 0; q < 6; ++q) { up[q] = u[q]; um[q] = u[q]; }
       up[k] += h;
       um[k] -= h;
-      adj_residual(i, d, p, a_nano, a_rest, up, n2, n3, b, th, t_eval, Gp);
-      adj_residual(i, d, p, a_nano, a_rest, um, n2, n3, b, th, t_eval, Gm);
+      adj_residual(i, d, p, a_nano, a_rest, up, n2, n3, b, th, t_eval, st, Gp);
+      adj_residual(i, d, p, a_nano, a_rest, um, n2, n3, b, th, t_eval, st, Gm);
       for (int r = 0; r < 6; ++r) J[r][k] = (Gp[r] - Gm[r]) / (2.0 * h);
     }
     // columns, Doppler parameter, log parameters
     double jn2[6], jn3[6], jb[6], jth[6 * kAdjParams];
     {
       const double h = kAdjStep * fmax(n2, 1e14);
-      adj_residual(i, d, p, a_nano, a_rest, u, n2 + h, n3, b, th, t_eval, Gp);
-      adj_residual(i, d, p, a_nano, a_rest, u, fmax(n2 - h, 0.0), n3, b, th, t_eval, Gm);
+      adj_residual(i, d, p, a_nano, a_rest, u, n2 + h, n3, b, th, t_eval, st, Gp);
+      adj_residual(i, d, p, a_nano, a_rest, u, fmax(n2 - h, 0.0), n3, b, th, t_eval, st, Gm);
       const double w = h + fmin(h, n2);
       for (int r = 0; r < 6; ++r) jn2[r] = (Gp[r] - Gm[r]) / w;
     }
     {
       const double h = kAdjStep * fmax(n3, 1e10);
-      adj_residual(i, d, p, a_nano, a_rest, u, n2, n3 + h, b, th, t_eval, Gp);
-      adj_residual(i, d, p, a_nano, a_rest, u, n2, fmax(n3 - h, 0.0), b, th, t_eval, Gm);
+      adj_residual(i, d, p, a_nano, a_rest, u, n2, n3 + h, b, th, t_eval, st, Gp);
+      adj_residual(i, d, p, a_nano, a_rest, u, n2, fmax(n3 - h, 0.0), b, th, t_eval, st, Gm);
       const double w = h + fmin(h, n3);
       for (int r = 0; r < 6; ++r) jn3[r] = (Gp[r] - Gm[r]) / w;
     }
     {
       const double h = kAdjStep * b;
-      adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b + h, th, t_eval, Gp);
-      adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b - h, th, t_eval, Gm);
+      adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b + h, th, t_eval, st, Gp);
+      adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b - h, th, t_eval, st, Gm);
       for (int r = 0; r < 6; ++r) jb[r] = (Gp[r] - Gm[r]) / (2.0 * h);
     }
     for (int k = 0; k < kAdjParams; ++k) {
       th[k] = kAdjStep;
-      adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b, th, t_eval, Gp);
+      adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b, th, t_eval, st, Gp);
       th[k] = -kAdjStep;
-      adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b, th, t_eval, Gm);
+      adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b, th, t_eval, st, Gm);
       th[k] = 0.0;
       for (int r = 0; r < 6; ++r) jth[r * kAdjParams + k] = (Gp[r] - Gm[r]) / (2.0 * kAdjStep);
     }
@@ -272,6 +294,7 @@ adj_local_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restric
     }
     for (int q = 0; q < 6 * kAdjParams; ++q) a.jth[6 * kAdjParams * i + q] = jth[q];
     a.jump[i] = jump ? 1 : 0;
+    a.teval[i] = t_eval;
   }
 }
 
@@ -375,6 +398,95 @@ __global__ void adj_grad_kernel(int64_t n, AdjArgs a, int k, double* __restrict_
     double s = 0.0;
     for (int r = 0; r < 6; ++r) s += a.lam[6 * i + r] * a.jth[6 * kAdjParams * i + r * kAdjParams + k];
     q[i] = -s;
+  }
+}
+
+// Gradient with respect to log n_H, local part: explicit loss term, the
+// cell's own residual, and its layers in the N_H2 / N_CO columns of the
+// cells downstream (cx2 / cx3 hold the strictly-upstream coupling of the
+// final lam).  Also the scalars lam . dG/d(G0, A_V, N_H) the ray scans
+// below need.
+__global__ void __launch_bounds__(128)
+adj_dens_local_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restrict__ a_nano,
+                      const double* __restrict__ a_rest, double b, double dx, AdjArgs a,
+                      double* __restrict__ qg0, double* __restrict__ qav,
+                      double* __restrict__ qnh) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double u[6] = {d.x_hi[i], d.x_h2[i], d.x_cp[i], d.x_c[i], d.x_co[i], d.t_gas[i]};
+    const double n2 = d.u_h2[i], n3 = d.u_co[i];
+    const double t_eval = a.teval[i];
+    const bool held = a.jump[i] != 0;
+    double th[kAdjParams];
+    for (int k = 0; k < kAdjParams; ++k) th[k] = 0.0;
+    double lam[6];
+    for (int r = 0; r < 6; ++r) lam[r] = a.lam[6 * i + r];
+    const AdjStatic st0 = adj_static(d, i);
+    double q[4];
+    for (int k = 0; k < 4; ++k) {
+      AdjStatic sp = st0, sm = st0;
+      double w;
+      if (k == 0) { sp.nh = st0.nh * exp(kAdjStep); sm.nh = st0.nh * exp(-kAdjStep); w = 2.0 * kAdjStep; }
+      else if (k == 1) { const double h = kAdjStep * st0.g0; sp.g0 += h; sm.g0 -= h; w = 2.0 * h; }
+      else if (k == 2) { const double h = kAdjStep * fmax(st0.av, 1.0); sp.av += h; sm.av -= h; w = 2.0 * h; }
+      else { const double h = kAdjStep * fmax(st0.nhc, 1e18); sp.nhc += h; sm.nhc = fmax(sm.nhc - h, 0.0); w = h + fmin(h, st0.nhc); }
+      double Gp[6], Gm[6];
+      adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b, th, t_eval, sp, Gp);
+      adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b, th, t_eval, sm, Gm);
+      double acc = 0.0;
+      for (int r = 0; r < (held ? 5 : 6); ++r) acc += lam[r] * (Gp[r] - Gm[r]) / w;
+      q[k] = acc;
+    }
+    double s2 = 0.0, s3 = 0.0;
+    for (int r = 0; r < 6; ++r) {
+      s2 += a.jn2[6 * i + r] * lam[r];
+      s3 += a.jn3[6 * i + r] * lam[r];
+    }
+    const double nh = st0.nh, dsn = d.ds[i] * nh;
+    double g = nh * dx * (a.w[0] * u[0] + a.w[1] * u[1] + a.w[2] * u[2] + a.w[3] * u[3] +
+                          a.w[4] * u[4]);
+    g -= q[0];
+    g -= u[1] * (a.cx2[i] + s2 * dsn);
+    g -= u[4] * (a.cx3[i] + 0.5 * s3 * dsn);
+    a.dn[i] = g;
+    qg0[i] = q[1];
+    qav[i] = q[2];
+    qnh[i] = q[3];
+  }
+}
+
+// Gradient with respect to log n_H through the ray march: for ray r, every
+// cell's G0 (if the ray carries external field) and, where r is the cell's
+// selected ray, its A_V and N_H depend on the densities upstream along r.
+// Reverse scan of the pencils of r's family: dn[c] -= n_c ds (sum over
+// downstream c' of a(c') + a(c) / 2), a(c') = lam . dG/d(G0, A_V, N_H) times
+// the derivative of those with respect to N_H,r(c').
+__global__ void adj_ray_scan_kernel(int axis, int fwd, int ray, double ds, double gw,
+                                    int64_t nx, int64_t ny, int64_t nz, int64_t n_pencils,
+                                    const double* __restrict__ dens, const int32_t* __restrict__ sel,
+                                    const double* __restrict__ qg0, const double* __restrict__ qav,
+                                    const double* __restrict__ qnh, double* __restrict__ dn) {
+  int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n_pencils) return;
+  int64_t base, stride, len;
+  if (axis == 0) { base = p; stride = ny * nz; len = nx; }
+  else if (axis == 1) { int64_t i = p / nz, k = p - i * nz; base = i * ny * nz + k; stride = nz; len = ny; }
+  else { base = p * nz; stride = 1; len = nz; }
+  double tot = 0.0;
+  for (int64_t t = 0; t < len; ++t) tot += dens[base + t * stride];
+  double suf = 0.0, acc = 0.0;
+  for (int64_t t = len - 1; t >= 0; --t) {  // reverse of the forward order
+    const int64_t c = base + (fwd ? t : (len - 1 - t)) * stride;
+    const double nc = dens[c];
+    const double nh_r = ds * (tot - suf - 0.5 * nc);  // upstream + own half layer
+    double a_c = 0.0;
+    if (nh_r > 0.0) {
+      if (gw != 0.0) a_c += qg0[c] * gw * exp(-1.8 * nh_r * kAVperNH) * (-1.8 * kAVperNH);
+      if (sel[c] == ray) a_c += qav[c] * kAVperNH + qnh[c];
+    }
+    dn[c] -= nc * ds * (acc + 0.5 * a_c);
+    acc += a_c;
+    suf += nc;
   }
 }
 

@@ -578,8 +578,8 @@ int p3d_steady_set_fixed_temperature(p3d_steady_t* h, int fixed) {
 }
 
 int p3d_steady_adjoint(p3d_steady_t* h, const double* w6, double dx, int64_t max_sweeps,
-                       double tol, double omega, double* grad9, double* loss2,
-                       int64_t* sweeps_out, int64_t* n_jump_out) {
+                       double tol, double omega, double* grad9, double* grad_ln_nh,
+                       double* loss2, int64_t* sweeps_out, int64_t* n_jump_out) {
   if (!h || !grad9 || !w6) return set_error(P3D_EINVAL, "null argument");
   if (max_sweeps < 1 || !(tol > 0.0) || !(dx > 0.0) || !(omega > 0.0 && omega <= 1.0))
     return set_error(P3D_EINVAL, "max_sweeps >= 1, tol > 0, dx > 0, 0 < omega <= 1 required");
@@ -618,15 +618,26 @@ int p3d_steady_adjoint(p3d_steady_t* h, const double* w6, double dx, int64_t max
   a.a3 = (double*)get(nd);
   a.qb = (double*)get(nd);
   a.jump = (int*)get(sizeof(int) * (size_t)n);
+  a.teval = (double*)get(nd);
+  a.dn = grad_ln_nh ? (double*)get(nd) : nullptr;
+  double* qg0 = grad_ln_nh ? (double*)get(nd) : nullptr;
+  double* qav = grad_ln_nh ? (double*)get(nd) : nullptr;
+  double* qnh = grad_ln_nh ? (double*)get(nd) : nullptr;
   a.red = (double*)get(sizeof(double) * (size_t)s->nparts);
   a.scal = (double*)get(sizeof(double) * 2);
   a.dmax = (unsigned long long*)get(sizeof(unsigned long long));
   unsigned int* n_bad = (unsigned int*)get(sizeof(unsigned int));
-  for (void* q : mem)
-    if (!q) {
+  {
+    const void* need[] = {a.jinv, a.jn2, a.jn3, a.jb, a.jth, a.lam, a.cx2, a.cx3, a.a2, a.a3,
+                          a.qb, a.jump, a.teval, a.red, a.scal, a.dmax, n_bad};
+    bool miss = false;
+    for (const void* q : need) miss = miss || !q;
+    if (grad_ln_nh) miss = miss || !a.dn || !qg0 || !qav || !qnh;
+    if (miss) {
       cleanup();
       return set_error(P3D_ENOMEM, "adjoint workspace (%lld cells)", (long long)n);
     }
+  }
   // columns and mean T of the final state
   const SteadyParams& par = s->par;
   int64_t dims[3] = {s->nx, s->ny, s->nz};
@@ -695,6 +706,30 @@ int p3d_steady_adjoint(p3d_steady_t* h, const double* w6, double dx, int64_t max
     dmax = gm > 0.0 ? dg / gm : dg;
     if (!std::isfinite(dmax)) break;
     if (dmax <= tol) break;
+  }
+  // gradient with respect to log n_H (optional)
+  if (grad_ln_nh) {
+    adj_couple_kernel<<<grid, kThreads, 0, str>>>(n, d, a);
+    for (int axis = 0; axis < 3; ++axis) {
+      int64_t np = n / dims[axis];
+      adj_scan_kernel<<<(unsigned)ceil_div(np, 128), 128, 0, str>>>(
+          axis, s->nx, s->ny, s->nz, np, s->dens, d.fam, a);
+    }
+    adj_dens_local_kernel<<<(unsigned)ceil_div(n, 128) < grid * 2u ? (unsigned)ceil_div(n, 128)
+                                                                  : grid * 2u,
+                            128, 0, str>>>(n, d, par, s->a_nano, s->a_rest, b, dx, a, qg0, qav,
+                                           qnh);
+    const RaySet& rs = s->rays;
+    for (int r = 0; r < rs.n; ++r) {
+      const int axis = rs.axis[r];
+      int64_t np = n / dims[axis];
+      adj_ray_scan_kernel<<<(unsigned)ceil_div(np, 128), 128, 0, str>>>(
+          axis, rs.fwd[r], r, rs.ds[r], rs.g_ext[r] * rs.w[r], s->nx, s->ny, s->nz, np,
+          s->dens, d.ray, qg0, qav, qnh, a.dn);
+    }
+    e = cudaMemcpyAsync(grad_ln_nh, a.dn, nd, cudaMemcpyDeviceToHost, str);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+    if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "adjoint density gradient"); }
   }
   double lc = 0.0, lt = 0.0;
   adj_loss_kernel<<<grid, kThreads, 0, str>>>(n, d, a, dx, a.cx2, a.cx3);

@@ -113,7 +113,7 @@ class PDRSolverGPU:
         L.call("p3d_steady_set_fixed_temperature", self._h, int(bool(fixed)))
 
     def adjoint(self, w_columns=(0.0, 0.0, 1.0, 1.0, 1.0), w_T=1.0, max_sweeps=20000, tol=1e-10,
-                omega=0.5):
+                omega=0.5, density_gradient=False):
         """Gradient of L = sum_cells n_H dx sum_s w_columns[s] x_s + w_T mean(T_gas)
         (s = x_HI, x_H2, x_C+, x_C, x_CO: weighted column sums over the grid)
         at the converged state with respect to the log rate multipliers
@@ -127,14 +127,18 @@ class PDRSolverGPU:
         loss = np.zeros(2)
         sw = L._i64(0)
         nj = L._i64(0)
+        gn = np.zeros(self.n_cells) if density_gradient else None
         rc = L.lib.p3d_steady_adjoint(self._h, L.dptr(w), self.cell_size, int(max_sweeps),
-                                      float(tol), float(omega), L.dptr(g), L.dptr(loss),
-                                      ctypes.byref(sw), ctypes.byref(nj))
+                                      float(tol), float(omega), L.dptr(g), L.dptr(gn),
+                                      L.dptr(loss), ctypes.byref(sw), ctypes.byref(nj))
         if rc != -5:  # P3D_ECONVERGE: tol not reached, results kept
             L.check("p3d_steady_adjoint", rc)
-        return {"grad": g, "loss_col": float(loss[0]), "loss_T": float(loss[1]),
-                "sweeps": int(sw.value), "n_jump": int(nj.value), "converged": rc == 0,
-                "message": "" if rc == 0 else L.lib.p3d_last_error().decode()}
+        out = {"grad": g, "loss_col": float(loss[0]), "loss_T": float(loss[1]),
+               "sweeps": int(sw.value), "n_jump": int(nj.value), "converged": rc == 0,
+               "message": "" if rc == 0 else L.lib.p3d_last_error().decode()}
+        if density_gradient:
+            out["grad_ln_nH"] = gn.reshape(self.nx, self.ny, self.nz)
+        return out
 
     def set(self, name, values):
         """Overwrite T_gas or one of x_HI, x_H2, x_Cp, x_C, x_CO on the device."""

@@ -32,6 +32,10 @@ struct SteadyDev {
   // diagnostics of the last iteration
   double *fh2, *gamma_pe, *t_dust;
   int32_t* flags;
+  // mixed thermal root: final node of the last full bisection (1024 + the
+  // ten decisions as bits) and its smallest certified margin |net| / sum|terms|
+  int16_t* bis_node;
+  float* bis_margin;
 };
 
 struct SteadyParams {

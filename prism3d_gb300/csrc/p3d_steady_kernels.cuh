@@ -110,6 +110,8 @@ ss_setup_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restrict
     d.b_last[i] = -1.0;
     d.chg_last[i] = INFINITY;
     d.flags[i] = 0;
+    d.bis_node[i] = 0;
+    d.bis_margin[i] = 0.0f;
   }
 }
 
@@ -386,12 +388,28 @@ ss_thermal_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
     c.n_o_nh = d.x_o[i] * nh;
     c.n_c_nh = x3 * nh;
     int tst = 0, nev = 0;
-    double troot = p.fix_t ? tg
-                   : MIXED ? root_mixed(c, p.lines, c_co_ss, p.theta2, c_lines32, c_co32,
-                                        g_bisect_mid, p.therm_tol_mixed, p.therm_max_iter,
-                                        d.t_root[i], &tst, &nev)
-                           : root_plain(c, p.lines, c_co_ss, p.theta2, p.therm_tol,
-                                        p.therm_max_iter, &tst, &nev);
+    double troot;
+    if (p.fix_t) {
+      troot = tg;
+    } else if (MIXED) {
+      // largest relative change of the root's inputs since the cell's last
+      // thermal solve: species, T (context), H2/CO columns, Doppler width
+      const double tp0 = d.t_prev[i];
+      double delta = fmax(d.chg_spec[i], tp0 > 0.0 ? fabs(tg - tp0) / tg : INFINITY);
+      delta = fmax(delta, fabs(d.u_h2[i] - d.u_h2_last[i]) / fmax(fabs(d.u_h2[i]), 1e-300));
+      delta = fmax(delta, fabs(d.u_co[i] - d.u_co_last[i]) / fmax(fabs(d.u_co[i]), 1e-300));
+      delta = fmax(delta, fabs(b_dop - d.b_last[i]) / b_dop);
+      int node = d.bis_node[i];
+      float margin = d.bis_margin[i];
+      troot = root_mixed(c, p.lines, c_co_ss, p.theta2, c_lines32, c_co32, g_bisect_mid,
+                         p.therm_tol_mixed, p.therm_max_iter, d.t_root[i], delta, &node, &margin,
+                         &tst, &nev);
+      d.bis_node[i] = (int16_t)node;
+      d.bis_margin[i] = margin;
+    } else {
+      troot = root_plain(c, p.lines, c_co_ss, p.theta2, p.therm_tol, p.therm_max_iter, &tst,
+                         &nev);
+    }
     my_evals += (unsigned long long)nev;
     my_fail += (unsigned)tst;
     double tp = d.t_prev[i], rp = d.r_prev[i], lo = d.t_lo[i], hi = d.t_hi[i], sp = d.span[i];

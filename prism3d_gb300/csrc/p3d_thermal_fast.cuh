@@ -251,29 +251,54 @@ __device__ __forceinline__ double root_plain(const ThermalCtx& c, const LinePara
 // and moves T by at most 1e-8 T (the slope error then bounds the remaining
 // error by ~1e-11 T); else a two-point FP64 check for a jump of the net
 // heating at T, else the safeguarded FP64 iteration of root_plain to tol.
+// A warm cell replays the last full bisection's decisions when its inputs
+// moved by less than margin / kReuseFactor (relative): the net heating's terms
+// then change by far less than the smallest certified |net| of those
+// decisions.
+constexpr double kReuseFactor = 300.0;
+
 __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LineParams& lp,
                                              const CoLevel* __restrict__ co, double theta2,
                                              const float* __restrict__ lines32,
                                              const float* __restrict__ co32,
                                              const double* __restrict__ mid_tab, double tol,
-                                             int max_it, double t_warm, int* status, int* n64) {
+                                             int max_it, double t_warm, double delta,
+                                             int* node_io, float* margin_io, int* status,
+                                             int* n64) {
   double K;
   const ThermalCtx32 f32 = make_ctx32(c, lp, co, &K);
   double t_lo = 10.0, t_hi = 1e5;
   int evals = 0;
-  int node = 1;
-  for (int k = 0; k < 10; ++k) {
-    double t_mid = __ldg(mid_tab + node);
-    float S;
-    float v = net_heating32(t_mid, f32, lines32, co32, co, &S);
-    bool pos;
-    if (fabsf(v) > kCertify * S) {
-      pos = v > 0.0f;
-    } else {
-      pos = net_heating_fast64(t_mid, c, lp, co, theta2) > 0.0;
-      ++evals;
+  if (*node_io >= 1024 && *node_io < 2048 && delta * kReuseFactor < (double)*margin_io) {
+    // the inputs moved too little to flip any of the last solve's decisions
+    // (each was certified with |net| >= margin sum|terms|): replay them
+    const int path = *node_io - 1024;
+    int node = 1;
+    for (int k = 0; k < 10; ++k) {
+      const double t_mid = __ldg(mid_tab + node);
+      if ((path >> (9 - k)) & 1) { t_lo = t_mid; node = 2 * node + 1; } else { t_hi = t_mid; node = 2 * node; }
     }
-    if (pos) { t_lo = t_mid; node = 2 * node + 1; } else { t_hi = t_mid; node = 2 * node; }
+  } else {
+    int node = 1;
+    float margin = INFINITY;
+    for (int k = 0; k < 10; ++k) {
+      double t_mid = __ldg(mid_tab + node);
+      float S;
+      float v = net_heating32(t_mid, f32, lines32, co32, co, &S);
+      bool pos;
+      if (fabsf(v) > kCertify * S) {
+        pos = v > 0.0f;
+        margin = fminf(margin, fabsf(v) / S);
+      } else {
+        const double f = net_heating_fast64(t_mid, c, lp, co, theta2);
+        pos = f > 0.0;
+        ++evals;
+        margin = fminf(margin, S > 0.0f ? (float)(fabs(f) / (double)S) : 0.0f);
+      }
+      if (pos) { t_lo = t_mid; node = 2 * node + 1; } else { t_hi = t_mid; node = 2 * node; }
+    }
+    *node_io = node;
+    *margin_io = margin == margin ? margin : 0.0f;
   }
   double t;
   if (t_warm > t_lo && t_warm < t_hi) {

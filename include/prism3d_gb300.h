@@ -379,7 +379,24 @@ int p3d_network_steady(p3d_network_t *net, int64_t n, const double *cond, double
 int p3d_network_steady_dev(p3d_network_t *net, int64_t n, const double *cond, double *x,
                            int32_t mixed, int32_t post, int32_t max_iter, double rtol,
                            int32_t *status, int32_t *iters, void *stream);
+int p3d_network_info(const p3d_network_t *net, int32_t *n_species, int32_t *reference_layout);
 int p3d_network_destroy(p3d_network_t *net);
+
+/* Refinement pass of a converged state with the full network (the BDF
+ * refine() of solver_3d.py:1056-1089): per cell n_H, T_gas, G0, A_V, zeta,
+ * f_shield_H2(N_H2, grid-mean T) and f_shield_CO(N_CO, N_H2) of the current
+ * state; initial abundances x_HI, x_H2, x_C+, x_C, x_CO, x_O, x_e of the
+ * state, x_OH = 1e-9 + 9e-8 f_H2 of the analytic initial state, x_H2O = 1e-8,
+ * x_HCO+ = 1e-10, the rest 1e-30 (solver_3d.py:134-136, 191); the network's
+ * steady state with post-processing (p3d_network_steady, mixed as given);
+ * the seven state abundances written back; then T_gas set to the thermal
+ * root (FP64 bisection + safeguarded Newton) with the new abundances.
+ * net must have the reference species layout.  cond_out (optional, host,
+ * n_cells x 7) receives the conditions passed to the network, x31_out
+ * (optional, host, n_cells x 31) and status_out (optional, host) the result.
+ * No counterpart entry point in the reference. */
+int p3d_steady_refine(p3d_steady_t *s, p3d_network_t *net, int32_t mixed, int32_t max_iter,
+                      double rtol, double *cond_out, double *x31_out, int32_t *status_out);
 
 #ifdef __cplusplus
 }

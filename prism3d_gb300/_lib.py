@@ -65,7 +65,9 @@ SIGNATURES = {
     "p3d_network_rhs_dev": [_vp, _i64, _D, _D, _D, _vp],
     "p3d_network_steady": [_vp, _i64, _D, _D, _i32, _i32, _i32, _f64, _I32, _I32],
     "p3d_network_steady_dev": [_vp, _i64, _D, _D, _i32, _i32, _i32, _f64, _I32, _I32, _vp],
+    "p3d_network_info": [_vp, _I32, _I32],
     "p3d_network_destroy": [_vp],
+    "p3d_steady_refine": [_vp, _vp, _i32, _i32, _f64, _D, _D, _I32],
 }
 _RESTYPES = {"p3d_version": ctypes.c_char_p, "p3d_last_error": ctypes.c_char_p}
 

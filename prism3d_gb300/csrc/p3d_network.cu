@@ -817,6 +817,13 @@ int p3d_network_create(p3d_network_t** out, int32_t n_species, int32_t n_reactio
   return P3D_OK;
 }
 
+int p3d_network_info(const p3d_network_t* h, int32_t* n_species, int32_t* reference_layout) {
+  if (!h) return set_error(P3D_EINVAL, "null network");
+  if (n_species) *n_species = h->host.ns;
+  if (reference_layout) *reference_layout = h->host.post_ok;
+  return P3D_OK;
+}
+
 int p3d_network_destroy(p3d_network_t* h) {
   if (!h) return P3D_OK;
   if (h->stream) cudaStreamSynchronize(h->stream);

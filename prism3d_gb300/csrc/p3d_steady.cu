@@ -404,7 +404,8 @@ int p3d_steady_get(p3d_steady_t* h, int field, double* host_out) {
     case P3D_F_N_H2:
     case P3D_F_N_CO: {
       ss_columns_out_kernel<<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(
-          s->n, field == P3D_F_N_H2 ? 1 : 0, s->dens, d.x_h2, d.ds, d.u_h2, d.u_co, s->scratch);
+          s->n, field == P3D_F_N_H2 ? 1 : 0, s->par.h2_implicit, s->dens, d.x_h2, d.ds, d.u_h2,
+          d.u_co, s->scratch);
       src = s->scratch;
       break;
     }
@@ -759,6 +760,81 @@ int p3d_steady_adjoint(p3d_steady_t* h, const double* w6, double dx, int64_t max
   if (!(dmax <= tol))
     return set_error(P3D_ECONVERGE, "adjoint sweeps did not reach tol (last relative gradient "
                      "change %.3e after %lld sweeps)", dmax, (long long)sweeps);
+  return P3D_OK;
+}
+
+int p3d_steady_refine(p3d_steady_t* h, p3d_network_t* net, int32_t mixed, int32_t max_iter,
+                      double rtol, double* cond_out, double* x31_out, int32_t* status_out) {
+  if (!h || !net) return set_error(P3D_EINVAL, "null argument");
+  int32_t ns = 0, ref = 0;
+  int rc = p3d_network_info(net, &ns, &ref);
+  if (rc) return rc;
+  if (ns != kNetSpecies || !ref)
+    return set_error(P3D_EINVAL, "refinement needs the reference 31-species network");
+  SteadySolver* s = &h->s;
+  if (s->iters_done < 1) return set_error(P3D_EINVAL, "run the steady state before refining it");
+  cudaStream_t str = s->st->stream;
+  const int64_t n = s->n;
+  const SteadyDev& d = s->d;
+  double *cond = nullptr, *x31 = nullptr;
+  int32_t* st = nullptr;
+  unsigned int* n_fail = nullptr;
+  auto cleanup = [&]() {
+    cudaStreamSynchronize(str);
+    cudaFree(cond);
+    cudaFree(x31);
+    cudaFree(st);
+    cudaFree(n_fail);
+  };
+  if (cudaMalloc(&cond, sizeof(double) * 7 * (size_t)n) != cudaSuccess ||
+      cudaMalloc(&x31, sizeof(double) * kNetSpecies * (size_t)n) != cudaSuccess ||
+      cudaMalloc(&st, sizeof(int32_t) * (size_t)n) != cudaSuccess ||
+      cudaMalloc(&n_fail, sizeof(unsigned int)) != cudaSuccess) {
+    cudaGetLastError();
+    cleanup();
+    return set_error(P3D_ENOMEM, "refinement workspace (%lld cells)", (long long)n);
+  }
+  // columns and Doppler width of the current state
+  const SteadyParams& par = s->par;
+  int64_t dims[3] = {s->nx, s->ny, s->nz};
+  for (int axis = 0; axis < 3; ++axis) {
+    int64_t np = n / dims[axis];
+    ss_columns_kernel<<<(unsigned)ceil_div(np, 128), 128, 0, str>>>(
+        axis, par.h2_implicit, s->nx, s->ny, s->nz, np, s->dens, d.x_h2, d.x_co, d.fam, d.ds,
+        d.u_h2, d.u_co);
+  }
+  ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(n, d.t_gas, s->parts);
+  ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, n, s->glob);
+  SteadyGlobals gl;
+  cudaError_t e = cudaMemcpyAsync(&gl, s->glob, sizeof(gl), cudaMemcpyDeviceToHost, str);
+  if (e == cudaSuccess) e = cudaMemsetAsync(n_fail, 0, sizeof(unsigned int), str);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+  if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "refinement setup"); }
+  const unsigned grid = grid_for(n, s->st->sms, 8);
+  ss_refine_gather_kernel<<<grid, kThreads, 0, str>>>(n, d, par, gl.b_dop, cond, x31);
+  if (cond_out) {
+    e = cudaMemcpyAsync(cond_out, cond, sizeof(double) * 7 * (size_t)n, cudaMemcpyDeviceToHost,
+                        str);
+    if (e != cudaSuccess) { cleanup(); return cuda_fail(e, "refinement conditions"); }
+  }
+  rc = p3d_network_steady_dev(net, n, cond, x31, mixed, 1, max_iter, rtol, st, nullptr, str);
+  if (rc) { cleanup(); return rc; }
+  ss_refine_scatter_kernel<<<grid, kThreads, 0, str>>>(n, d, par, x31, s->a_nano, s->a_rest,
+                                                       n_fail);
+  unsigned int fails = 0;
+  e = cudaGetLastError();
+  if (e == cudaSuccess && x31_out)
+    e = cudaMemcpyAsync(x31_out, x31, sizeof(double) * kNetSpecies * (size_t)n,
+                        cudaMemcpyDeviceToHost, str);
+  if (e == cudaSuccess && status_out)
+    e = cudaMemcpyAsync(status_out, st, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, str);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&fails, n_fail, sizeof(fails), cudaMemcpyDeviceToHost, str);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+  cleanup();
+  if (e != cudaSuccess) return cuda_fail(e, "refinement");
+  s->launches += 7;
+  if (fails) return set_error(P3D_ECONVERGE, "refinement: %u thermal roots not converged", fails);
   return P3D_OK;
 }
 

@@ -448,16 +448,18 @@ ss_thermal_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
   }
 }
 
-// N_H2 (which = 1) or N_CO (which = 0) of the selected ray for output:
-// N_H2 adds the cell's own half layer to the upstream sum.
-__global__ void ss_columns_out_kernel(int64_t n, int which, const double* __restrict__ dens,
+// N_H2 (which = 1) or N_CO (which = 0) of the selected ray for output; with
+// own_implicit the H2 column excludes the cell's own half layer (solved inside
+// the chemistry) and it is added here.
+__global__ void ss_columns_out_kernel(int64_t n, int which, int own_implicit,
+                                      const double* __restrict__ dens,
                                       const double* __restrict__ xh2,
                                       const double* __restrict__ ds,
                                       const double* __restrict__ u_h2,
                                       const double* __restrict__ u_co, double* __restrict__ out) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = which ? u_h2[i] + ds[i] * dens[i] * xh2[i] : u_co[i];
+    out[i] = which ? u_h2[i] + (own_implicit ? ds[i] * dens[i] * xh2[i] : 0.0) : u_co[i];
 }
 
 // hist[kHistCols it ...] = (largest relative change, chemistry failures,
@@ -495,6 +497,102 @@ __global__ void ss_reset_globals_kernel(SteadyGlobals* g) {
     g->n_active = 0u;
     g->iter = 0;
   }
+}
+
+// ------------------------------------------------------------ refinement
+// Reference species layout of the full network (prism3d/chemistry/solver.py:28-36).
+constexpr int kNetSpecies = 31;
+constexpr int kNetE = 0, kNetH = 1, kNetH2 = 2, kNetCp = 7, kNetC = 8, kNetCO = 9, kNetO = 13,
+              kNetOH = 15, kNetH2O = 17, kNetHCOp = 22;
+
+// Conditions (n x 7) and initial abundances (n x 31) of the refinement pass.
+__global__ void ss_refine_gather_kernel(int64_t n, SteadyDev d, SteadyParams p, double b_dop,
+                                        double* __restrict__ cond, double* __restrict__ x31) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double nh = d.dens[i];
+    const double nh2 = p.h2_implicit ? d.u_h2[i] + d.ds[i] * nh * d.x_h2[i] : d.u_h2[i];
+    double d1, dh;
+    double* c = cond + 7 * i;
+    c[0] = nh;
+    c[1] = d.t_gas[i];
+    c[2] = d.g0[i];
+    c[3] = d.av[i];
+    c[4] = d.zeta[i];
+    c[5] = fsh_h2(nh2, b_dop, &d1);
+    c[6] = fsh_co(d.u_co[i], nh2, &dh);
+    double* x = x31 + (int64_t)kNetSpecies * i;
+    for (int k = 0; k < kNetSpecies; ++k) x[k] = 1e-30;
+    x[kNetE] = d.x_e[i];
+    x[kNetH] = d.x_hi[i];
+    x[kNetH2] = d.x_h2[i];
+    x[kNetCp] = d.x_cp[i];
+    x[kNetC] = d.x_c[i];
+    x[kNetCO] = d.x_co[i];
+    x[kNetO] = d.x_o[i];
+    const double lg = log10(fmax(d.g0[i], 0.1));
+    const double fh2_ic = 0.5 * (1.0 + tanh((d.av[i] - (1.5 + 0.3 * lg)) / 0.8));
+    x[kNetOH] = 1e-9 + 9e-8 * fmin(fmax(fh2_ic, 0.0), 1.0);
+    x[kNetH2O] = 1e-8;
+    x[kNetHCOp] = p.x_hcop;
+  }
+}
+
+// Write the refined abundances back and set T_gas to the thermal root with
+// them (dust coupling and PE heating at the current T).
+__global__ void __launch_bounds__(kThreads)
+ss_refine_scatter_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restrict__ x31,
+                         const double* __restrict__ a_nano, const double* __restrict__ a_rest,
+                         unsigned int* n_fail) {
+  unsigned int fails = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double* x = x31 + (int64_t)kNetSpecies * i;
+    const double x0 = x[kNetH], x1 = x[kNetH2], x3 = x[kNetC], xe = x[kNetE];
+    d.x_hi[i] = x0;
+    d.x_h2[i] = x1;
+    d.x_cp[i] = x[kNetCp];
+    d.x_c[i] = x3;
+    d.x_co[i] = x[kNetCO];
+    d.x_o[i] = x[kNetO];
+    d.x_e[i] = xe;
+    const double nh = d.dens[i];
+    const double tg = d.t_gas[i];
+    const double gpe = pe_cell(p.pe, a_nano, a_rest, d.g0[i], tg, xe, nh, p.f_nano, p.e_g);
+    const double td = tdust(d.td_rad[i], nh, tg);
+    const double rh2 = h2_form(tg, td, p.f_nano, p.sigma_nano, p.sigma_lc, p.sigma_sil);
+    const double zeta = d.zeta[i];
+    const double uv = d.uv0[i] * d.fh2[i];
+    ThermalCtx c;
+    double gf = gpe;
+    gf += 3.3e-11 * uv * x1 * nh * (0.4 * kEVtoErg);
+    gf += rh2 * x0 * (nh * nh) * (1.5 * kEVtoErg);
+    gf += 3.0e-10 * uv * x1 * nh * (2.0 * kEVtoErg) * (nh / (nh + 3e4));
+    gf += zeta * (x0 + 2.0 * x1) * nh * (20.0 * kEVtoErg);
+    gf += d.hci0[i] * x3 * nh * kEVtoErg;
+    c.gamma_fixed = gf;
+    const double mu = x1 > 0.5 ? 2.0 : 1.0;
+    c.gg_coeff = 2.0 * 0.35 * 1e-21 * (nh * nh) * sqrt(8.0 * kKBoltz / (kPi * mu * kMH)) * kKBoltz;
+    c.t_dust = td;
+    c.n_e = xe * nh;
+    c.n_hi = x0 * nh;
+    c.n_h2 = x1 * nh;
+    c.n_co = x[kNetCO] * nh;
+    c.n_cp_nh = x[kNetCp] * nh;
+    c.n_o_nh = x[kNetO] * nh;
+    c.n_c_nh = x3 * nh;
+    int tst = 0, nev = 0;
+    const double troot = root_plain(c, p.lines, c_co_ss, p.theta2, p.therm_tol,
+                                    p.therm_max_iter, &tst, &nev);
+    fails += (unsigned)tst;
+    d.t_gas[i] = troot;
+    d.t_root[i] = troot;
+    d.gamma_pe[i] = gpe;
+    d.t_dust[i] = td;
+    d.chg_last[i] = INFINITY;  // the mixed path re-solves every cell next
+  }
+  for (int o = 16; o > 0; o >>= 1) fails += __shfl_xor_sync(0xffffffffu, fails, o);
+  if ((threadIdx.x & 31) == 0 && fails) atomicAdd(n_fail, fails);
 }
 
 }  // namespace p3d

@@ -107,6 +107,35 @@ class PDRSolverGPU:
             raise ValueError("rate scale needs 8 values")
         L.call("p3d_steady_set_rate_scale", self._h, L.dptr(sc))
 
+    def refine(self, network=None, mixed=True, rtol=1e-8, max_iter=300, return_species=False,
+               return_conditions=False):
+        """Refinement pass with the full 31-species network (the reference's
+        BDF refine(), solver_3d.py:1056-1089): every cell's network steady
+        state from the current conditions and abundances, written back, then
+        T_gas re-solved.  Returns the per-cell network status (0 =
+        converged), then with return_species the (nx, ny, nz, 31) abundances
+        and with return_conditions the (n_cells, 7) conditions used."""
+        from .network import ChemistrySolverGPU
+        own = network is None
+        net = ChemistrySolverGPU() if own else network
+        x = np.empty((self.n_cells, 31)) if return_species else None
+        cond = np.empty((self.n_cells, 7)) if return_conditions else None
+        st = np.empty(self.n_cells, np.int32)
+        try:
+            rc = L.lib.p3d_steady_refine(self._h, net._h, int(bool(mixed)), int(max_iter),
+                                         float(rtol), L.dptr(cond), L.dptr(x), L.iptr(st))
+            if rc != -5:  # P3D_ECONVERGE: results kept, status says which cells
+                L.check("p3d_steady_refine", rc)
+        finally:
+            if own:
+                net.close()
+        out = [st.reshape(self.nx, self.ny, self.nz)]
+        if return_species:
+            out.append(x.reshape(self.nx, self.ny, self.nz, 31))
+        if return_conditions:
+            out.append(cond)
+        return out[0] if len(out) == 1 else tuple(out)
+
     def set_fixed_temperature(self, fixed=True):
         """Hold T_gas at its current values in later run() calls (chemistry
         and shielding only) or solve the thermal balance again."""

@@ -227,6 +227,22 @@ def run_gb300(args, ws, rank, local):
         "gpu_launches": int(sum(launches)),
         "clocks": clk.summary(),
     }
+    # column-density maps of the converged state (observation pipeline), host
+    # clock around the C-ABI call (device work, small D2H of the maps)
+    from prism3d_gb300.observations import column_density_maps
+    s2b = PDRSolverGPU(dens, box, G0_external=g0, zeta_CR_0=zeta, nside_rt=nside, T_init=100.0)
+    s2b.run(max_iterations=13, convergence_tol=1e-300, mixed=True, n_allow=0, w_chem=args.w_chem)
+    tms = []
+    for _ in range(4):
+        t0 = time.perf_counter()
+        column_density_maps(s2b, los_axis=2, inclination_deg=0.0)
+        tms.append(time.perf_counter() - t0)
+    s2b.close()
+    tm = min(tms[1:])
+    out["column_maps"] = {"ms": 1e3 * tm, "bytes_read": 40 * n,
+                          "GB_per_s": 40 * n / tm / 1e9,
+                          "note": "5 fields read once (n_H, x_H2, x_CO, x_C+, x_e), LOS = z, "
+                                  "host clock around p3d_steady_column_maps"}
     out["cpu_baseline"] = cpu_baseline(args, dens, g0, nside, zeta, cell, float(np.mean(iters)))
     if args.network_cells > 0:
         out["network"] = network_bench(args)

@@ -398,6 +398,29 @@ int p3d_network_destroy(p3d_network_t *net);
 int p3d_steady_refine(p3d_steady_t *s, p3d_network_t *net, int32_t mixed, int32_t max_iter,
                       double rtol, double *cond_out, double *x31_out, int32_t *status_out);
 
+/* ---------------------------------------------------------------------
+ * Column-density maps (observations/jwst_pipeline.py:109-180): sums along
+ * los_axis (0, 1, 2) times cell_size of n_H, 2 n_H x_H2, n_H x_CO, n_H x_C+,
+ * n_H x_e, and A_V_total = 5.34e-22 N_H; maps = 6 consecutive 2-D maps of
+ * the grid shape without the LOS axis (C order).  |inclination_deg| >= 0.01
+ * shears LOS slice t by tan(i) (t - n_los / 2) pixels along the first other
+ * axis with linear interpolation, 0 outside (jwst_pipeline.py:472-520).
+ * p3d_integrate_column: one field, no shear (integrate_column).
+ * No counterpart entry points in the reference (NumPy there).
+ * ------------------------------------------------------------------- */
+int p3d_column_maps(int64_t nx, int64_t ny, int64_t nz, const double *density, const double *x_h2,
+                    const double *x_co, const double *x_cp, const double *x_e, double cell_size,
+                    int32_t los_axis, double inclination_deg, double *maps);
+int p3d_column_maps_dev(int64_t nx, int64_t ny, int64_t nz, const double *density,
+                        const double *x_h2, const double *x_co, const double *x_cp,
+                        const double *x_e, double cell_size, int32_t los_axis,
+                        double inclination_deg, double *maps, void *stream);
+int p3d_integrate_column(int64_t nx, int64_t ny, int64_t nz, const double *field,
+                         double cell_size, int32_t los_axis, double *out);
+/* The maps of a steady-state handle's current state (host output). */
+int p3d_steady_column_maps(p3d_steady_t *s, double cell_size, int32_t los_axis,
+                           double inclination_deg, double *maps);
+
 #ifdef __cplusplus
 }
 #endif

@@ -749,3 +749,49 @@ def net_heating_at(ctx, t, lines=None):
         from prism3d_gb300.tables import line_params
         lines = line_params()
     return net_heating(ctx, np.ascontiguousarray(t).ravel(), *lines)
+
+
+# ---------------------------------------------------------------------------
+# Column-density maps (prism3d/observations/jwst_pipeline.py:109-180, 472-520)
+# ---------------------------------------------------------------------------
+def _shift_first_axis(sl, dx):
+    """2D slice shifted by dx along its first axis: linear interpolation,
+    0 where the source position falls outside [0, n - 1] (the reference's
+    scipy.ndimage.shift(order=1, mode='constant'))."""
+    n = sl.shape[0]
+    src = np.arange(n, dtype=np.float64) - dx
+    out = np.zeros_like(sl)
+    ok = (src >= 0.0) & (src <= n - 1)
+    i0 = np.floor(src[ok]).astype(np.int64)
+    w = src[ok] - i0
+    i1 = np.minimum(i0 + 1, n - 1)
+    out[ok] = (1.0 - w)[:, None] * sl[i0] + w[:, None] * sl[i1]
+    return out
+
+
+def shear(data, los_axis, inclination_deg):
+    """jwst_pipeline.py:472-520: slice i along the LOS shifted by
+    tan(inclination) (i - n_los / 2) pixels along the first other axis."""
+    if abs(inclination_deg) < 0.01:
+        return data
+    t = np.tan(np.radians(inclination_deg))
+    out = np.empty_like(data)
+    n_los = data.shape[los_axis]
+    for i in range(n_los):
+        dx = t * (i - n_los / 2.0)
+        idx = [slice(None)] * 3
+        idx[los_axis] = i
+        out[tuple(idx)] = _shift_first_axis(data[tuple(idx)], dx)
+    return out
+
+
+def column_density_maps(density, x_H2, x_CO, x_Cp, x_e, cell_size, los_axis=2,
+                        inclination_deg=0.0):
+    """jwst_pipeline.py:134-180: N_H, N_H2, N_CO, N_Cp, N_e, A_V_total."""
+    def integ(f):
+        return np.sum(shear(f, los_axis, inclination_deg), axis=los_axis) * cell_size
+    m = {"N_H": integ(density), "N_H2": integ(density * x_H2 * 2),
+         "N_CO": integ(density * x_CO), "N_Cp": integ(density * x_Cp),
+         "N_e": integ(density * x_e)}
+    m["A_V_total"] = m["N_H"] * AV_per_NH
+    return m

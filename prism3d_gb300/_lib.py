@@ -66,6 +66,10 @@ SIGNATURES = {
     "p3d_network_steady": [_vp, _i64, _D, _D, _i32, _i32, _i32, _f64, _I32, _I32],
     "p3d_network_steady_dev": [_vp, _i64, _D, _D, _i32, _i32, _i32, _f64, _I32, _I32, _vp],
     "p3d_network_info": [_vp, _I32, _I32],
+    "p3d_column_maps": [_i64, _i64, _i64] + [_D] * 5 + [_f64, _i32, _f64, _D],
+    "p3d_column_maps_dev": [_i64, _i64, _i64] + [_D] * 5 + [_f64, _i32, _f64, _D, _vp],
+    "p3d_integrate_column": [_i64, _i64, _i64, _D, _f64, _i32, _D],
+    "p3d_steady_column_maps": [_vp, _f64, _i32, _f64, _D],
     "p3d_network_destroy": [_vp],
     "p3d_steady_refine": [_vp, _vp, _i32, _i32, _f64, _D, _D, _I32],
 }

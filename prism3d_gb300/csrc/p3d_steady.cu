@@ -838,6 +838,33 @@ int p3d_steady_refine(p3d_steady_t* h, p3d_network_t* net, int32_t mixed, int32_
   return P3D_OK;
 }
 
+int p3d_steady_column_maps(p3d_steady_t* h, double cell_size, int32_t los_axis,
+                           double inclination_deg, double* maps) {
+  if (!h || !maps) return set_error(P3D_EINVAL, "null argument");
+  SteadySolver* s = &h->s;
+  if (los_axis < 0 || los_axis > 2) return set_error(P3D_EINVAL, "los_axis must be 0, 1 or 2");
+  const int64_t dims[3] = {s->nx, s->ny, s->nz};
+  const int64_t npix = s->n / dims[los_axis];
+  double* out = nullptr;
+  cudaError_t e = cudaMalloc(&out, sizeof(double) * 6 * (size_t)npix);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(P3D_ENOMEM, "column maps output");
+  }
+  const SteadyDev& d = s->d;
+  int rc = p3d_column_maps_dev(s->nx, s->ny, s->nz, s->dens, d.x_h2, d.x_co, d.x_cp, d.x_e,
+                               cell_size, los_axis, inclination_deg, out, s->st->stream);
+  if (!rc) {
+    e = cudaMemcpyAsync(maps, out, sizeof(double) * 6 * (size_t)npix, cudaMemcpyDeviceToHost,
+                        s->st->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->st->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "steady column maps");
+  }
+  cudaStreamSynchronize(s->st->stream);
+  cudaFree(out);
+  return rc;
+}
+
 int p3d_steady_destroy(p3d_steady_t* h) {
   delete h;
   return P3D_OK;

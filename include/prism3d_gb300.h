@@ -179,6 +179,18 @@ int p3d_fuv_field_3d(int64_t nx, int64_t ny, int64_t nz, const double *density,
                      const double *weights, int64_t n_rays, double *g0, double *a_v,
                      double *n_h_col, double *n_h2_col, double *n_co_col, int32_t *ray_out);
 
+/* FUV field of an embedded point source (fuv_rt_3d.py:74-212,
+ * compute_fuv_field_point_source): star_pos (3, cm), L_fuv (erg/s),
+ * x_h2 / x_co may be NULL (zero abundances).  Outputs as p3d_fuv_field_3d. */
+int p3d_fuv_point_source(int64_t nx, int64_t ny, int64_t nz, const double *density,
+                         const double *x_h2, const double *x_co, const double *star_pos,
+                         double L_fuv, double cell_size, double *g0, double *a_v, double *n_h,
+                         double *n_h2, double *n_co);
+int p3d_fuv_point_source_dev(int64_t nx, int64_t ny, int64_t nz, const double *density,
+                             const double *x_h2, const double *x_co, const double *star_pos,
+                             double L_fuv, double cell_size, double *g0, double *a_v,
+                             double *n_h, double *n_h2, double *n_co, void *stream);
+
 int p3d_fuv_field_3d_dev(int64_t nx, int64_t ny, int64_t nz, const double *density,
                          const double *x_h2, const double *x_co, const double *g0_ext,
                          int64_t n_g0, double cell_size, const double *dirs,
@@ -397,6 +409,14 @@ int p3d_network_destroy(p3d_network_t *net);
  * No counterpart entry point in the reference. */
 int p3d_steady_refine(p3d_steady_t *s, p3d_network_t *net, int32_t mixed, int32_t max_iter,
                       double rtol, double *cond_out, double *x31_out, int32_t *status_out);
+
+/* One grain-state step per cell (solver_3d.py:465-507, _evolve_dust_state):
+ * f_nano and e_g updated in place from G0 and n_H.  No counterpart entry
+ * point in the reference (NumPy there). */
+int p3d_evolve_dust_state(int64_t n, const double *g0, const double *n_h, double *f_nano,
+                          double *e_g);
+int p3d_evolve_dust_state_dev(int64_t n, const double *g0, const double *n_h, double *f_nano,
+                              double *e_g, void *stream);
 
 /* ---------------------------------------------------------------------
  * Column-density maps (observations/jwst_pipeline.py:109-180): sums along

@@ -795,3 +795,76 @@ def column_density_maps(density, x_H2, x_CO, x_Cp, x_e, cell_size, los_axis=2,
          "N_e": integ(density * x_e)}
     m["A_V_total"] = m["N_H"] * AV_per_NH
     return m
+
+
+# ---------------------------------------------------------------------------
+# Point-source FUV field (prism3d/radiative_transfer/fuv_rt_3d.py:74-212)
+# ---------------------------------------------------------------------------
+G0_TO_FLUX = 1.6e-3  # prism3d/utils/constants.py:45
+
+
+def _star_columns(layer, axis, s):
+    """Column from the star's plane s outward along one axis: cells above s
+    sum the layers s .. i-1, cells below sum i+1 .. s (the star cell's own
+    layer included, the cell's excluded); cells in the plane get 0."""
+    a = np.moveaxis(layer, axis, 0)
+    out = np.zeros_like(a)
+    acc = np.zeros_like(a[0])
+    for i in range(s, a.shape[0] - 1):
+        acc = acc + a[i]
+        out[i + 1] = acc
+    acc = np.zeros_like(a[0])
+    for i in range(s, 0, -1):
+        acc = acc + a[i]
+        out[i - 1] = acc
+    return np.moveaxis(out, 0, axis)
+
+
+def fuv_point_source(density, star_pos, L_FUV, cell_size, x_H2=None, x_CO=None):
+    """(G0, A_V, N_H, N_H2, N_CO) of an embedded star: per-axis columns from
+    the star's planes, the column of the dominant displacement axis scaled
+    by min(r / |d_dom|, 3), midpoint correction, G0 = L / (4 pi r^2 F_Habing)
+    exp(-1.8 A_V)."""
+    nx, ny, nz = density.shape
+    x_H2 = np.zeros_like(density) if x_H2 is None else x_H2
+    x_CO = np.zeros_like(density) if x_CO is None else x_CO
+    sx, sy, sz = (float(v) for v in star_pos)
+    c = [(np.arange(m) + 0.5) * cell_size for m in (nx, ny, nz)]
+    dx = c[0][:, None, None] - sx
+    dy = c[1][None, :, None] - sy
+    dz = c[2][None, None, :] - sz
+    dx, dy, dz = np.broadcast_arrays(dx, dy, dz)
+    r = np.maximum(np.sqrt(dx ** 2 + dy ** 2 + dz ** 2), 0.5 * cell_size)
+    star = [int(np.clip(p / cell_size, 0, m - 1)) for p, m in zip((sx, sy, sz), (nx, ny, nz))]
+    layers = (density * cell_size, density * x_H2 * 2.0 * cell_size, density * x_CO * cell_size)
+    ax, ay, az = np.abs(dx), np.abs(dy), np.abs(dz)
+    dom_x = (ax >= ay) & (ax >= az)
+    dom_y = (ay > ax) & (ay >= az)
+    dom = np.where(dom_x, 0, np.where(dom_y, 1, 2))
+    ddom = np.choose(dom, (ax, ay, az))
+    pc = np.minimum(r / np.maximum(ddom, 0.5 * cell_size), 3.0)
+    out = []
+    for lay in layers:
+        cols = [_star_columns(lay, a, star[a]) for a in range(3)]
+        tot = np.choose(dom, cols) * pc
+        out.append(np.maximum(tot - 0.5 * lay * pc, 0.0))
+    av = out[0] * AV_per_NH
+    g0 = L_FUV / (4.0 * np.pi * r ** 2 * G0_TO_FLUX) * np.exp(-1.8 * av)
+    return g0, av, out[0], out[1], out[2]
+
+
+# ---------------------------------------------------------------------------
+# Grain-state step (prism3d/solver_3d.py:465-507)
+# ---------------------------------------------------------------------------
+def evolve_dust_state(G0, nH, f_nano, E_g):
+    """One 10 kyr THEMIS grain step: destruction / replenishment / accretion
+    of f_nano, relaxation of E_g; returns (f_nano, E_g)."""
+    dt = 1e4 * 3.15e7
+    f_dest = np.exp(-dt / (1e4 * 3.15e7 / np.maximum(G0 / 1e4, 0.01)))
+    f_rep = np.minimum(dt / (1e6 * 3.15e7), 0.1)
+    f_acc = np.where((G0 < 1) & (nH > 1e4), np.minimum(dt / (1e5 * 3.15e7 * 1e4 / nH), 0.1), 0.0)
+    fn = np.clip(f_nano * f_dest + (1.0 - f_nano) * f_rep + f_acc, 0.01, 2.0)
+    tau = 1e3 * 3.15e7 / np.maximum(G0, 0.01)
+    eq = np.where(G0 > 10, 0.01, np.minimum(0.1 + 0.5 * np.log10(np.maximum(nH, 1.0)), 2.5))
+    eg = np.clip(E_g + (eq - E_g) * np.minimum(dt / tau, 1.0), 0.01, 2.5)
+    return fn, eg

@@ -42,6 +42,10 @@ SIGNATURES = {
                         [_I32],
     "p3d_fuv_field_3d_dev": [_i64, _i64, _i64, _D, _D, _D, _D, _i64, _f64, _D, _D, _i64] +
                             [_D] * 5 + [_I32, _vp],
+    "p3d_evolve_dust_state": [_i64, _D, _D, _D, _D],
+    "p3d_evolve_dust_state_dev": [_i64, _D, _D, _D, _D, _vp],
+    "p3d_fuv_point_source": [_i64, _i64, _i64, _D, _D, _D, _D, _f64, _f64] + [_D] * 5,
+    "p3d_fuv_point_source_dev": [_i64, _i64, _i64, _D, _D, _D, _D, _f64, _f64] + [_D] * 5 + [_vp],
     "p3d_steady_create": [ctypes.POINTER(_vp), _i64, _i64, _i64, _D, _D, _i64, _f64, _D, _D, _i64,
                           _f64, _f64, _f64, _f64, _D, _i64, _f64, _f64, _i64, _f64, _f64, _i64,
                           _D, _D, _D, _D, _D, _D, _D, _D],

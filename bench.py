@@ -174,6 +174,19 @@ def run_gb300(args, ws, rank, local):
         tp = time.perf_counter() - t0
         plain = {"value": n / tp, "unit": "cells/s", "iterations": s.iterations,
                  "converged": bool(okp), "seconds": tp, "sample": "full solve"}
+        # per-species difference of the mixed state (the e2e solve) from the
+        # plain FP64 state, cells with the plain value above 1e-20
+        err = {}
+        for k, a in zip(("T_gas", "x_HI", "x_H2", "x_Cp", "x_C", "x_CO", "x_O", "x_e"), outs):
+            b = s.get(k).ravel()
+            a = a.ravel()
+            m = np.abs(b) > 1e-20
+            rel = np.abs(a - b)[m] / np.abs(b)[m]
+            err[k] = {"frac_le_1e-6": float(np.mean(rel <= 1e-6)),
+                      "frac_le_1e-4": float(np.mean(rel <= 1e-4)),
+                      "median": float(np.median(rel)), "p99": float(np.percentile(rel, 99)),
+                      "max": float(rel.max())}
+        plain["mixed_vs_plain_rel_error"] = err
     else:
         k = args.plain_iters
         t0 = time.perf_counter()
@@ -218,7 +231,8 @@ def run_gb300(args, ws, rank, local):
                      "algorithmic_flops_per_launch": FP64_OPS_PER_CELL_SOLVE * n,
                      "per_unit": f"{FP64_OPS_PER_CELL_SOLVE:.0f} FP64 flops per cell solve "
                                  "(ncu instruction counts, profiles/cell_kernels_slab96.md)"},
-        "roofline_hbm": {"kernel": "ss_columns_kernel (3 axis passes, one outer iteration)",
+        "roofline_hbm": {"kernel": "ss_columns_all_kernel (3 axes x 2 directions, one launch per "
+                                   "outer iteration)",
                          "bound": "hbm", "achieved": col_gbs, "peak": hbm, "unit": "GB/s",
                          "frac": col_gbs / hbm, "traffic": None, "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": col_bytes},

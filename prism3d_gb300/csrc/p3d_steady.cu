@@ -71,16 +71,20 @@ struct SteadySolver {
   }
 };
 
+// Selected-ray N_H2 / N_CO columns of every cell: one launch, one thread per
+// (axis, direction, pencil).
+static void launch_columns(SteadySolver* s, const SteadyParams& par, cudaStream_t str) {
+  const SteadyDev& d = s->d;
+  const int64_t total = 2 * (s->ny * s->nz + s->nx * s->nz + s->nx * s->ny);
+  ss_columns_all_kernel<<<(unsigned)ceil_div(total, 128), 128, 0, str>>>(
+      par.h2_implicit, s->nx, s->ny, s->nz, s->dens, d.x_h2, d.x_co, d.fam, d.ds, d.u_h2,
+      d.u_co);
+}
+
 static int launch_iteration(SteadySolver* s, bool mixed, const SteadyParams& par,
                             cudaStream_t str) {
   const SteadyDev& d = s->d;
-  int64_t dims[3] = {s->nx, s->ny, s->nz};
-  for (int axis = 0; axis < 3; ++axis) {
-    int64_t np = s->n / dims[axis];
-    ss_columns_kernel<<<(unsigned)ceil_div(np, 128), 128, 0, str>>>(
-        axis, par.h2_implicit, s->nx, s->ny, s->nz, np, s->dens, d.x_h2, d.x_co, d.fam, d.ds,
-        d.u_h2, d.u_co);
-  }
+  launch_columns(s, par, str);
   ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(s->n, d.t_gas, s->parts);
   ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, s->n, s->glob);
   unsigned grid = grid_for(s->n, s->st->sms, 4);
@@ -100,7 +104,7 @@ static int launch_iteration(SteadySolver* s, bool mixed, const SteadyParams& par
   return e == cudaSuccess ? P3D_OK : cuda_fail(e, "steady iteration launch");
 }
 
-constexpr int kLaunchesPerIteration = 9;  // mixed; the plain path launches 8
+constexpr int kLaunchesPerIteration = 7;  // mixed; the plain path launches 6
 
 }  // namespace p3d
 
@@ -478,18 +482,12 @@ int p3d_steady_kernel_times(p3d_steady_t* h, int reps, double* ms4) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  int64_t dims[3] = {s->nx, s->ny, s->nz};
   unsigned grid = grid_for(s->n, s->st->sms, 4);
   for (int which = 0; which < 4; ++which) {
     cudaEventRecord(e0, str);
     for (int r = 0; r < reps; ++r) {
       if (which == 0) {
-        for (int axis = 0; axis < 3; ++axis) {
-          int64_t np = s->n / dims[axis];
-          ss_columns_kernel<<<(unsigned)ceil_div(np, 128), 128, 0, str>>>(
-              axis, par.h2_implicit, s->nx, s->ny, s->nz, np, s->dens, d.x_h2, d.x_co, d.fam,
-              d.ds, d.u_h2, d.u_co);
-        }
+        launch_columns(s, par, str);
       } else if (which == 1) {
         ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(s->n, d.t_gas, s->parts);
         ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, s->n, s->glob);
@@ -643,12 +641,7 @@ int p3d_steady_adjoint(p3d_steady_t* h, const double* w6, double dx, int64_t max
   // columns and mean T of the final state
   const SteadyParams& par = s->par;
   int64_t dims[3] = {s->nx, s->ny, s->nz};
-  for (int axis = 0; axis < 3; ++axis) {
-    int64_t np = n / dims[axis];
-    ss_columns_kernel<<<(unsigned)ceil_div(np, 128), 128, 0, str>>>(
-        axis, par.h2_implicit, s->nx, s->ny, s->nz, np, s->dens, d.x_h2, d.x_co, d.fam, d.ds,
-        d.u_h2, d.u_co);
-  }
+  launch_columns(s, par, str);
   ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(n, d.t_gas, s->parts);
   ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, n, s->glob);
   SteadyGlobals gl;
@@ -796,13 +789,7 @@ int p3d_steady_refine(p3d_steady_t* h, p3d_network_t* net, int32_t mixed, int32_
   }
   // columns and Doppler width of the current state
   const SteadyParams& par = s->par;
-  int64_t dims[3] = {s->nx, s->ny, s->nz};
-  for (int axis = 0; axis < 3; ++axis) {
-    int64_t np = n / dims[axis];
-    ss_columns_kernel<<<(unsigned)ceil_div(np, 128), 128, 0, str>>>(
-        axis, par.h2_implicit, s->nx, s->ny, s->nz, np, s->dens, d.x_h2, d.x_co, d.fam, d.ds,
-        d.u_h2, d.u_co);
-  }
+  launch_columns(s, par, str);
   ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(n, d.t_gas, s->parts);
   ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, n, s->glob);
   SteadyGlobals gl;

@@ -152,6 +152,67 @@ ss_columns_kernel(int axis, int own_implicit, int64_t nx, int64_t ny, int64_t nz
   }
 }
 
+// All three axes and both directions in one launch, one thread per
+// (axis, direction, pencil): six times the threads of one axis pass, so
+// every SM holds several warps of independent scans.  Same sums in the same
+// order as ss_columns_kernel.
+__global__ void __launch_bounds__(128)
+ss_columns_all_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz,
+                      const double* __restrict__ dens, const double* __restrict__ xh2,
+                      const double* __restrict__ xco, const int8_t* __restrict__ fam,
+                      const double* __restrict__ ds, double* __restrict__ u_h2,
+                      double* __restrict__ u_co) {
+  const int64_t p0 = ny * nz, p1 = nx * nz, p2 = nx * ny;
+  const int64_t total = 2 * (p0 + p1 + p2);
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int fwd = (int)(q & 1);
+    int64_t p = q >> 1;
+    int axis;
+    if (p < p0) axis = 0;
+    else if (p < p0 + p1) { axis = 1; p -= p0; }
+    else { axis = 2; p -= p0 + p1; }
+    int64_t base, stride, len;
+    if (axis == 0) { base = p; stride = ny * nz; len = nx; }
+    else if (axis == 1) { int64_t i = p / nz, k = p - i * nz; base = i * ny * nz + k; stride = nz; len = ny; }
+    else { base = p * nz; stride = 1; len = nz; }
+    const int8_t want = (int8_t)(axis * 2 + fwd);
+    double s2 = 0.0, s3 = 0.0;
+    constexpr int kU = 8;  // loads of kU cells issued before their sequential sums
+    for (int64_t t0 = 0; t0 < len; t0 += kU) {
+      double nv[kU], hv[kU], cv[kU];
+      int8_t fv[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int64_t t = t0 + u;
+        if (t < len) {
+          const int64_t c = base + (fwd ? t : (len - 1 - t)) * stride;
+          nv[u] = dens[c];
+          hv[u] = xh2[c];
+          cv[u] = xco[c];
+          fv[u] = fam[c];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const int64_t t = t0 + u;
+        if (t < len) {
+          const int64_t c = base + (fwd ? t : (len - 1 - t)) * stride;
+          const double l2 = nv[u] * hv[u] * 2.0;
+          const double l3 = nv[u] * cv[u];
+          if (fv[u] == want) {
+            const double dsc = ds[c];
+            u_h2[c] = own_implicit ? dsc * s2 : fmax(dsc * (s2 + 0.5 * l2), 0.0);
+            u_co[c] = fmax(dsc * (s3 + 0.5 * l3), 0.0);
+          }
+          s2 += l2;
+          s3 += l3;
+        }
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------------ reductions
 __global__ void ss_sum_kernel(int64_t n, const double* __restrict__ x, double* __restrict__ part) {
   __shared__ double sh[kThreads / 32];

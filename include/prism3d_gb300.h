@@ -313,6 +313,12 @@ int p3d_steady_set_fixed_temperature(p3d_steady_t *s, int fixed);
 int p3d_steady_adjoint(p3d_steady_t *s, const double *w6, double dx, int64_t max_sweeps,
                        double tol, double omega, double *grad9, double *grad_ln_nh,
                        double *loss2, int64_t *sweeps_out, int64_t *n_jump_out);
+/* Pick the launch shape of the per-cell chemistry and thermal kernels:
+ * {128, 256} threads per block x {2, 4, 8, 16, 32, 64} blocks per SM, each timed
+ * (CUDA events, every cell solved) on the state after warm_iters mixed
+ * iterations; the fastest is kept for later runs.  Resets the state before
+ * returning.  cfg_out (optional): threads, blocks per SM; ms_out: its time. */
+int p3d_steady_autotune(p3d_steady_t *s, int warm_iters, int32_t *cfg_out, double *ms_out);
 /* Kernels launched on the device since the last p3d_steady_reset. */
 int p3d_steady_launch_count(p3d_steady_t *s, int64_t *out);
 /* Mean time (ms) over reps launches on the current state of: the three

@@ -44,6 +44,9 @@ struct SteadySolver {
   int graph_mixed = -1;
   SteadyParams graph_par;
   int64_t iters_done = 0;
+  // launch shape of the per-cell chemistry / thermal kernels (threads per
+  // block, blocks per SM of the grid-stride loop); p3d_steady_autotune sets it
+  int cell_threads = kThreads, cell_per_sm = 4;
   int64_t launches = 0;  // kernels launched since the last reset
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;  // reset .. end of last run
   double last_dmax = INFINITY;
@@ -71,6 +74,15 @@ struct SteadySolver {
   }
 };
 
+// Grid of the per-cell kernels: grid-stride loops, at most per_sm blocks of
+// `threads` threads per SM.
+static unsigned cell_grid(int64_t n, int sms, int threads, int per_sm) {
+  int64_t b = ceil_div(n, threads);
+  const int64_t cap = (int64_t)sms * per_sm;
+  if (b > cap) b = cap;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
 // Selected-ray N_H2 / N_CO columns of every cell: one launch, one thread per
 // (axis, direction, pencil).
 static void launch_columns(SteadySolver* s, const SteadyParams& par, cudaStream_t str) {
@@ -87,17 +99,16 @@ static int launch_iteration(SteadySolver* s, bool mixed, const SteadyParams& par
   launch_columns(s, par, str);
   ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(s->n, d.t_gas, s->parts);
   ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, s->n, s->glob);
-  unsigned grid = grid_for(s->n, s->st->sms, 4);
+  const int bt = s->cell_threads;
+  const unsigned grid = cell_grid(s->n, s->st->sms, bt, s->cell_per_sm);
   if (mixed) {
     ss_mark_kernel<true><<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(s->n, d, par,
                                                                               s->glob);
-    ss_chem_kernel<true><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->a_nano,
-                                                     s->a_rest);
-    ss_thermal_kernel<true><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob);
+    ss_chem_kernel<true><<<grid, bt, 0, str>>>(s->n, d, par, s->glob, s->a_nano, s->a_rest);
+    ss_thermal_kernel<true><<<grid, bt, 0, str>>>(s->n, d, par, s->glob);
   } else {
-    ss_chem_kernel<false><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->a_nano,
-                                                      s->a_rest);
-    ss_thermal_kernel<false><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob);
+    ss_chem_kernel<false><<<grid, bt, 0, str>>>(s->n, d, par, s->glob, s->a_nano, s->a_rest);
+    ss_thermal_kernel<false><<<grid, bt, 0, str>>>(s->n, d, par, s->glob);
   }
   ss_record_kernel<<<1, 32, 0, str>>>(s->glob, s->hist, kMaxHist);
   cudaError_t e = cudaGetLastError();
@@ -482,7 +493,8 @@ int p3d_steady_kernel_times(p3d_steady_t* h, int reps, double* ms4) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  unsigned grid = grid_for(s->n, s->st->sms, 4);
+  const int bt = s->cell_threads;
+  const unsigned grid = cell_grid(s->n, s->st->sms, bt, s->cell_per_sm);
   for (int which = 0; which < 4; ++which) {
     cudaEventRecord(e0, str);
     for (int r = 0; r < reps; ++r) {
@@ -495,13 +507,12 @@ int p3d_steady_kernel_times(p3d_steady_t* h, int reps, double* ms4) {
         ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, s->n, s->glob);
         ss_mark_kernel<true><<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(s->n, d, par,
                                                                                   s->glob);
-        ss_chem_kernel<true><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->a_nano,
-                                                         s->a_rest);
-        ss_thermal_kernel<true><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob);
+        ss_chem_kernel<true><<<grid, bt, 0, str>>>(s->n, d, par, s->glob, s->a_nano, s->a_rest);
+        ss_thermal_kernel<true><<<grid, bt, 0, str>>>(s->n, d, par, s->glob);
       } else {
-        ss_chem_kernel<false><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob, s->a_nano,
-                                                          s->a_rest);
-        ss_thermal_kernel<false><<<grid, kThreads, 0, str>>>(s->n, d, par, s->glob);
+        ss_chem_kernel<false><<<grid, bt, 0, str>>>(s->n, d, par, s->glob, s->a_nano,
+                                                    s->a_rest);
+        ss_thermal_kernel<false><<<grid, bt, 0, str>>>(s->n, d, par, s->glob);
       }
     }
     cudaEventRecord(e1, str);
@@ -560,6 +571,68 @@ int p3d_fp64_peak_tflops(double* tflops) {
   if (e != cudaSuccess) return cuda_fail(e, "fp64 peak probe");
   *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
   return P3D_OK;
+}
+
+int p3d_steady_autotune(p3d_steady_t* h, int warm_iters, int32_t* cfg_out, double* ms_out) {
+  if (!h || warm_iters < 1 || warm_iters > 64)
+    return set_error(P3D_EINVAL, "autotune: null handle or warm_iters outside [1, 64]");
+  SteadySolver* s = &h->s;
+  cudaStream_t str = s->st->stream;
+  // a representative state: warm_iters mixed iterations from the initial one
+  int rc = p3d_steady_reset(h);
+  if (rc) return rc;
+  rc = p3d_steady_run(h, 1, warm_iters, 1e-300, 0, 0.1, 0.5, nullptr, nullptr);
+  if (rc && rc != P3D_ECONVERGE) return rc;
+  SteadyParams par = s->par;
+  par.count_thr[0] = par.count_thr[1] = par.count_thr[2] = 1.0;
+  par.quiet_tol = 0.0;  // every cell solved
+  par.quiet_in_tol = 0.0;
+  par.w_chem = 0.1;
+  const SteadyDev& d = s->d;
+  const int threads[2] = {128, 256};
+  const int per_sm[6] = {2, 4, 8, 16, 32, 64};
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = INFINITY;
+  int bt = s->cell_threads, bp = s->cell_per_sm;
+  cudaError_t e = cudaSuccess;
+  for (int a = 0; a < 2 && e == cudaSuccess; ++a)
+    for (int b = 0; b < 6 && e == cudaSuccess; ++b) {
+      const unsigned grid = cell_grid(s->n, s->st->sms, threads[a], per_sm[b]);
+      float ms = 0.f, tot = 0.f;
+      for (int rep = 0; rep < 3; ++rep) {  // first launch warms, two timed
+        cudaEventRecord(e0, str);
+        ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, s->n, s->glob);
+        ss_mark_kernel<true><<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(s->n, d, par,
+                                                                                  s->glob);
+        ss_chem_kernel<true><<<grid, threads[a], 0, str>>>(s->n, d, par, s->glob, s->a_nano,
+                                                           s->a_rest);
+        ss_thermal_kernel<true><<<grid, threads[a], 0, str>>>(s->n, d, par, s->glob);
+        cudaEventRecord(e1, str);
+        e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) break;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0) tot += ms;
+      }
+      if (e == cudaSuccess && tot / 2 < best) {
+        best = tot / 2;
+        bt = threads[a];
+        bp = per_sm[b];
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return cuda_fail(e, "autotune");
+  s->cell_threads = bt;
+  s->cell_per_sm = bp;
+  if (s->graph) {  // baked the old launch shape
+    cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+  }
+  if (cfg_out) { cfg_out[0] = bt; cfg_out[1] = bp; }
+  if (ms_out) *ms_out = best;
+  return p3d_steady_reset(h);
 }
 
 int p3d_steady_set_rate_scale(p3d_steady_t* h, const double* scale8) {

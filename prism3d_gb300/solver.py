@@ -96,6 +96,17 @@ class PDRSolverGPU:
         L.check("p3d_steady_run", rc)
         return True
 
+    def autotune(self, warm_iterations=13):
+        """Time the per-cell kernels' launch shapes on a representative state
+        and keep the fastest (threads per block, blocks per SM); resets the
+        solver.  Returns (threads, blocks_per_sm, ms)."""
+        cfg = np.zeros(2, np.int32)
+        ms = L._f64(0.0)
+        L.call("p3d_steady_autotune", self._h, int(warm_iterations), L.iptr(cfg),
+               ctypes.byref(ms))
+        self.iterations = 0
+        return int(cfg[0]), int(cfg[1]), float(ms.value)
+
     RATE_NAMES = ("H2_formation", "H2_photodiss", "H2_cr_destruction", "C_photoion",
                   "Cp_recombination", "CO_photodiss", "CO_cr_dissociation", "C_OH_to_CO")
 

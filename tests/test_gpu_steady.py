@@ -79,3 +79,17 @@ def test_converged_state_is_fixed_point(mixed):
             r[f] = (G2 - T * f)[off]
         jump = (r[1 - 1e-7] > 0) & (r[1 + 1e-7] < 0)
         assert np.sum(~jump) <= max(2, int(1e-3 * T.size)), (int(off.sum()), int(np.sum(~jump)))
+
+
+def test_autotune_keeps_results():
+    """The launch shape changes no per-cell arithmetic: a solve after
+    autotuning reproduces the untuned one exactly."""
+    s, _ = _solver("cube16")
+    s.run(max_iterations=12, convergence_tol=1e-300, mixed=True, n_allow=0)
+    ref = {k: s.get(k) for k in SPECIES + ("T_gas",)}
+    threads, per_sm, ms = s.autotune(warm_iterations=5)
+    assert threads in (128, 256) and per_sm in (2, 4, 8, 16, 32, 64) and ms > 0
+    s.run(max_iterations=12, convergence_tol=1e-300, mixed=True, n_allow=0)
+    for k, v in ref.items():
+        np.testing.assert_array_equal(s.get(k), v)
+    s.close()

@@ -165,6 +165,7 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   p.h2_implicit = 0;
   for (int k = 0; k < 8; ++k) p.rs[k] = 1.0;
   p.fix_t = 0;
+  p.quiet_tol = p.quiet_in_tol = p.quiet_b_tol = 0.0;
   p.pe = PeGrid{log_psi_min, log_psi_step, eg_min, eg_step, (int)n_psi, (int)n_eg};
   memcpy(p.lines.cii, cii, sizeof(p.lines.cii));
   memcpy(p.lines.oi63, oi63, sizeof(p.lines.oi63));
@@ -313,6 +314,9 @@ int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, in
   par.count_thr[2] = tol * 0.01;
   par.quiet_tol = tol * 0.01;
   par.quiet_in_tol = tol * 0.1;
+  // b ~ sqrt(mean T); a cell's state moves by at most ~ its relative change,
+  // so drift below tol leaves it within the tolerance of its fixed point
+  par.quiet_b_tol = tol;
   auto conv = [&](const double* hrow) {
     return hrow[0] < tol || (double)hrow[4] <= (double)n_allow;
   };
@@ -490,6 +494,7 @@ int p3d_steady_kernel_times(p3d_steady_t* h, int reps, double* ms4) {
   par.count_thr[0] = par.count_thr[1] = par.count_thr[2] = 1.0;
   par.quiet_tol = 0.0;  // no compaction: every cell solved
   par.quiet_in_tol = 0.0;
+  par.quiet_b_tol = 0.0;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -587,6 +592,7 @@ int p3d_steady_autotune(p3d_steady_t* h, int warm_iters, int32_t* cfg_out, doubl
   par.count_thr[0] = par.count_thr[1] = par.count_thr[2] = 1.0;
   par.quiet_tol = 0.0;  // every cell solved
   par.quiet_in_tol = 0.0;
+  par.quiet_b_tol = 0.0;
   par.w_chem = 0.1;
   const SteadyDev& d = s->d;
   const int threads[2] = {128, 256};

@@ -48,7 +48,8 @@ struct SteadyParams {
   int h2_implicit;  // 1: the cell's own H2 half layer is solved implicitly
   double count_thr[3];  // thresholds of the n_gt counters
   double quiet_tol;     // mixed path: skip cells whose last change was <= this
-  double quiet_in_tol;  // ... and whose inputs moved <= this since
+  double quiet_in_tol;  // ... and whose columns moved <= this since
+  double quiet_b_tol;   // ... and whose Doppler width moved <= this since
   // multipliers of the reduced network's rate coefficients (1 = the
   // reference's): H2 formation, H2 photodissociation, H2 cosmic-ray
   // destruction, C photoionisation, C+ recombination, CO photodissociation,

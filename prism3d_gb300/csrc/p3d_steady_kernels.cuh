@@ -304,9 +304,11 @@ __device__ __forceinline__ double t_update(double t_in, double G, double w_t, do
 // ----------------------------------------------------------- cell kernel
 // ------------------------------------------------------------ worklist
 // A cell is solved this iteration unless (mixed path, from the fourth
-// iteration on) its last solve changed it by <= quiet_tol and its inputs --
-// selected-ray columns, Doppler width -- have moved by <= quiet_in_tol since:
-// then it is at its fixed point to ~tol / 10 and keeps its state.  Solved
+// iteration on) its last solve changed it by <= quiet_tol and its inputs
+// have moved little since: its selected-ray columns by <= quiet_in_tol, the
+// Doppler width (set by the grid-mean T, which drifts slowly while the last
+// cells settle) by <= quiet_b_tol.  Then it is at its fixed point to about
+// the tolerance and keeps its state.  Solved
 // cells are appended to a dense list (one atomic per warp), so the chemistry
 // and thermal kernels run full warps of active cells.
 template <bool MIXED>
@@ -325,7 +327,7 @@ ss_mark_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
       const double uh2 = d.u_h2[i], uco = d.u_co[i];
       if (d.chg_last[i] <= q && fabs(uh2 - d.u_h2_last[i]) <= qi * fabs(uh2) &&
           fabs(uco - d.u_co_last[i]) <= qi * fabs(uco) &&
-          fabs(b_dop - d.b_last[i]) <= qi * b_dop)
+          fabs(b_dop - d.b_last[i]) <= p.quiet_b_tol * b_dop)
         active = false;
     }
     const unsigned m = __ballot_sync(0xffffffffu, active);

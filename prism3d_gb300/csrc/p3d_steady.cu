@@ -515,6 +515,7 @@ int p3d_steady_kernel_times(p3d_steady_t* h, int reps, double* ms4) {
         ss_chem_kernel<true><<<grid, bt, 0, str>>>(s->n, d, par, s->glob, s->a_nano, s->a_rest);
         ss_thermal_kernel<true><<<grid, bt, 0, str>>>(s->n, d, par, s->glob);
       } else {
+        ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, s->n, s->glob);
         ss_chem_kernel<false><<<grid, bt, 0, str>>>(s->n, d, par, s->glob, s->a_nano,
                                                     s->a_rest);
         ss_thermal_kernel<false><<<grid, bt, 0, str>>>(s->n, d, par, s->glob);

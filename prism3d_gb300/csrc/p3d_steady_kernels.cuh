@@ -244,6 +244,7 @@ __global__ void ss_finalize_kernel(int nparts, const double* __restrict__ part, 
   g->therm_fail = 0u;
   g->n_gt[0] = g->n_gt[1] = g->n_gt[2] = 0u;
   g->n_active = 0u;
+  g->therm_next = 0u;
 }
 
 __device__ __forceinline__ void block_max_atomic(double v, unsigned long long* dst) {
@@ -423,8 +424,17 @@ ss_thermal_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
   unsigned int my_gt[3] = {0u, 0u, 0u};
   unsigned int my_fail = 0u;
   unsigned long long my_evals = 0ull;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count;
-       k += (int64_t)gridDim.x * blockDim.x) {
+  // Warps take 32 cells (mixed: list entries) at a time from a global
+  // counter, so the uneven root-finding work spreads over all warps until
+  // none is left.
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned int base = 0u;
+    if (lane == 0) base = atomicAdd(&g->therm_next, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if ((int64_t)base >= count) break;
+    const int64_t k = (int64_t)base + lane;
+    if (k >= count) continue;
     const int64_t i = MIXED ? (int64_t)d.list[k] : k;
     const double nh = d.dens[i];
     const double tg = d.t_gas[i];
@@ -558,6 +568,7 @@ __global__ void ss_reset_globals_kernel(SteadyGlobals* g) {
     g->therm_fail = 0u;
     g->n_gt[0] = g->n_gt[1] = g->n_gt[2] = 0u;
     g->n_active = 0u;
+  g->therm_next = 0u;
     g->iter = 0;
   }
 }

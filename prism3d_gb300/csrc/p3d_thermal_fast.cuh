@@ -30,7 +30,7 @@ __device__ __forceinline__ double line64(double q, const double* l, double inv_t
   return r_lu / (r_lu + r_ul) * l[1] * kHPlanck * l[0];
 }
 
-__device__ __forceinline__ double net_heating_fast64(double t, const ThermalCtx& c,
+__device__ __forceinline__ double net_heating_fast64_body(double t, const ThermalCtx& c,
                                                      const LineParams& lp,
                                                      const CoLevel* __restrict__ co,
                                                      double theta2) {
@@ -92,6 +92,16 @@ __device__ __forceinline__ double net_heating_fast64(double t, const ThermalCtx&
   return net;
 }
 
+// Out of line for the mixed root, which calls it from several places: one
+// copy keeps the mixed thermal kernel within the instruction cache.  The
+// plain root inlines the body.
+__device__ __noinline__ double net_heating_fast64(double t, const ThermalCtx& c,
+                                                  const LineParams& lp,
+                                                  const CoLevel* __restrict__ co,
+                                                  double theta2) {
+  return net_heating_fast64_body(t, c, lp, co, theta2);
+}
+
 // Per-cell FP32 coefficients, scaled by 1 / Gamma_fixed.
 struct ThermalCtx32 {
   float gg, td, ne, nhi, nh2, cii, o63, o145, ci609, ci370, co, h2, lya, rec;
@@ -132,7 +142,7 @@ __device__ __forceinline__ float line32(float q, float a_ul, float t_ul, float g
 // Branch points (the CO ladder break, T >= 100 K, T >= 3000 K) are decided
 // on the FP64 temperature t64 so the FP32 and FP64 functions switch terms at
 // the same temperatures.
-__device__ __forceinline__ float net_heating32(double t64, const ThermalCtx32& f,
+__device__ __noinline__ float net_heating32(double t64, const ThermalCtx32& f,
                                                const float* __restrict__ lines32,
                                                const float* __restrict__ co32,
                                                const CoLevel* __restrict__ co, float* S) {
@@ -213,16 +223,16 @@ __device__ __forceinline__ double root_plain(const ThermalCtx& c, const LinePara
   double t_lo = 10.0, t_hi = 1e5;
   for (int k = 0; k < 10; ++k) {
     double t_mid = sqrt(t_lo * t_hi);
-    if (net_heating_fast64(t_mid, c, lp, co, theta2) > 0.0) t_lo = t_mid; else t_hi = t_mid;
+    if (net_heating_fast64_body(t_mid, c, lp, co, theta2) > 0.0) t_lo = t_mid; else t_hi = t_mid;
   }
   int evals = 10;
   double t = sqrt(t_lo * t_hi);
   double dx_old = t_hi - t_lo, dx = dx_old;
   *status = 1;
   for (int k = 0; k < max_it; ++k) {
-    double f = net_heating_fast64(t, c, lp, co, theta2);
+    double f = net_heating_fast64_body(t, c, lp, co, theta2);
     double eps = t * 1e-7;
-    double df = (net_heating_fast64(t + eps, c, lp, co, theta2) - f) / eps;
+    double df = (net_heating_fast64_body(t + eps, c, lp, co, theta2) - f) / eps;
     evals += 2;
     if (f > 0.0) t_lo = t; else t_hi = t;
     if (f == 0.0) { *status = 0; break; }

@@ -69,6 +69,7 @@ struct SteadyGlobals {
   unsigned int n_gt[3];  // cells with relative change > count_thr[k]
   unsigned int n_active;  // cells solved this iteration (length of the list)
   unsigned int therm_next;  // thermal kernel: next cell (mixed: list entry) to hand out
+  unsigned int chem_next;   // chemistry kernel: the same
   int iter;
 };
 

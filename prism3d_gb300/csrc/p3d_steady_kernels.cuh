@@ -245,6 +245,7 @@ __global__ void ss_finalize_kernel(int nparts, const double* __restrict__ part, 
   g->n_gt[0] = g->n_gt[1] = g->n_gt[2] = 0u;
   g->n_active = 0u;
   g->therm_next = 0u;
+  g->chem_next = 0u;
 }
 
 __device__ __forceinline__ void block_max_atomic(double v, unsigned long long* dst) {
@@ -351,8 +352,14 @@ ss_chem_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g,
   const int iter = g->iter;
   const int64_t count = MIXED ? (int64_t)g->n_active : n;
   unsigned int my_fail = 0u;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < count;
-       k += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  for (;;) {  // 32 cells per warp from a global counter (as the thermal kernel)
+    unsigned int base = 0u;
+    if (lane == 0) base = atomicAdd(&g->chem_next, 32u);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if ((int64_t)base >= count) break;
+    const int64_t k = (int64_t)base + lane;
+    if (k >= count) continue;
     const int64_t i = MIXED ? (int64_t)d.list[k] : k;
     const double nh = d.dens[i];
     const double tg = d.t_gas[i];
@@ -569,6 +576,7 @@ __global__ void ss_reset_globals_kernel(SteadyGlobals* g) {
     g->n_gt[0] = g->n_gt[1] = g->n_gt[2] = 0u;
     g->n_active = 0u;
   g->therm_next = 0u;
+  g->chem_next = 0u;
     g->iter = 0;
   }
 }

@@ -233,7 +233,10 @@ def run_gb300(args, ws, rank, local):
                      "peak_source": "measured live: DFMA-chain kernel on this GPU",
                      "algorithmic_flops_per_launch": FP64_OPS_PER_CELL_SOLVE * n,
                      "per_unit": f"{FP64_OPS_PER_CELL_SOLVE:.0f} FP64 flops per cell solve "
-                                 "(ncu instruction counts, profiles/cell_kernels_slab96.md)"},
+                                 "(ncu instruction counts, profiles/cell_kernels_slab96.md)",
+                     "fp64_pipe_active_ncu": "85-87% (chemistry and thermal kernels, "
+                                             "profiles/cell_kernels_slab96.md): the pipe also "
+                                             "runs FP64 compares, min/max and conversions"},
         "roofline_hbm": {"kernel": "ss_columns_all_kernel (3 axes x 2 directions, one launch per "
                                    "outer iteration)",
                          "bound": "hbm", "achieved": col_gbs, "peak": hbm, "unit": "GB/s",

@@ -83,6 +83,18 @@ WORKLOADS = {
 }
 
 
+# name -> one-line description (bench config)
+WORKLOAD_DESC = {
+    "cube16": "16^3 log-normal cube, mean n_H 1e4, sigma_ln 1.0, G0 1e4 on -x, 12 rays",
+    "cube64": "64^3 log-normal cube, mean n_H 1e4, sigma_ln 1.5, G0 1e3 on -x, 48 rays",
+    "slab128": "128^3 tanh-ramp slab 1e3->1e5 x lognormal 0.8, G0=2.6e4 on -x, 48 rays",
+    "cube32": "32^3 log-normal cube, mean n_H 3e4, sigma_ln 1.0, G0 1e4 on -x, 12 rays",
+    "slab256": "256^3 tanh-ramp slab 1e3->3e5 x lognormal 1.2 + Gaussian cores (1e6), "
+               "G0=2.6e4 on -x, 48 rays, zeta 5e-16",
+    "slab96": "96^3 tanh-ramp slab 1e3->1e5 x lognormal 0.8, G0=2.6e4 on -x, 48 rays",
+}
+
+
 def network_cells(n, seed=1):
     """Per-cell conditions (n, 7: n_H, T, G0, A_V, zeta, f_sh_H2, f_sh_CO) for
     the full-network benchmark: log-uniform n_H 10-3e6 cm^-3, T 10-1e4 K, G0

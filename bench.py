@@ -48,6 +48,18 @@ if ROOT not in sys.path:
 METRIC = "converged cells/sec at 128^3 (batched mixed vs plain FP64 GPU, <=1e-6 rel err)"
 
 
+def max_over_ranks(value, ws, device="cpu"):
+    """Largest value over the ranks of the process group (the step time of the
+    slowest replica); the value itself with one rank."""
+    if ws <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -148,11 +160,7 @@ def run_gb300(args, ws, rank, local):
             launches.append(s.launch_count())
     if ws > 1:
         torch.distributed.barrier()
-    t_step = float(np.mean(times))
-    if ws > 1:
-        tt = torch.tensor([t_step], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = max_over_ranks(float(np.mean(times)), ws, "cuda")
     value = n * ws / t_step
     hist = s.convergence_history()
     # e2e through the C ABI from host buffers
@@ -421,7 +429,8 @@ def main():
     if ws > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
+        if args.impl == "gb300":
+            torch.cuda.set_device(local)
         dist.init_process_group("nccl" if args.impl == "gb300" else "gloo")
     if args.impl == "reference":
         out = run_reference(args, ws, rank)

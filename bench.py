@@ -171,6 +171,21 @@ def run_gb300(args, ws, rank, local):
            w_chem=args.w_chem)
     outs = [s2.get(k) for k in ("T_gas", "x_HI", "x_H2", "x_Cp", "x_C", "x_CO", "x_O", "x_e")]
     t_e2e = time.perf_counter() - t0
+    refine = None
+    if args.network_cells > 0:
+        # refinement pass with the full network on the converged state (the
+        # reference's BDF refine(), solver_3d.py:1056-1089), device time
+        from prism3d_gb300.network import ChemistrySolverGPU
+        net = ChemistrySolverGPU()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st_ref = s2.refine(network=net, mixed=True)
+        t_ref = time.perf_counter() - t0
+        net.close()
+        refine = {"value": n / t_ref, "unit": "cells/s", "seconds": t_ref,
+                  "unconverged_frac": float((st_ref != 0).mean()),
+                  "sample": "every cell of the converged grid, host clock around "
+                            "p3d_steady_refine (gather, network, scatter, thermal root)"}
     s2.close()
     h2d = dens.nbytes + 8 * (s.tables.pe_table.size + 3 * s.tables.n_bins + 60)
     d2h = sum(a.nbytes for a in outs)
@@ -274,6 +289,7 @@ def run_gb300(args, ws, rank, local):
     out["cpu_baseline"] = cpu_baseline(args, dens, g0, nside, zeta, cell, float(np.mean(iters)))
     if args.network_cells > 0:
         out["network"] = network_bench(args)
+        out["network"]["refine_pass"] = refine
     return out
 
 

@@ -328,7 +328,7 @@ __global__ void adj_couple_kernel(int64_t n, SteadyDev d, AdjArgs a) {
   }
 }
 
-// Transpose of ss_columns_kernel: for each pencil and direction, cells
+// Transpose of ss_columns_all_kernel: for each pencil and direction, cells
 // upstream of a cell of that family receive its a2 / a3 (suffix sums).
 __global__ void adj_scan_kernel(int axis, int64_t nx, int64_t ny, int64_t nz, int64_t n_pencils,
                                 const double* __restrict__ dens, const int8_t* __restrict__ fam,

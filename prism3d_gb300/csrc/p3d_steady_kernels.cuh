@@ -115,47 +115,15 @@ ss_setup_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restrict
   }
 }
 
-// --------------------------------------------------------------- columns
-// Thread per pencil of `axis`; both directions.  For cells whose selected
-// ray has this axis and direction: u_h2 = N_H2 and u_co = N_CO, the
-// reference's columns with the cell's own half layer (fuv_rt_3d.py:334-388);
-// with own_implicit the own H2 half layer is left out of u_h2 and added
-// inside the chemistry solve.
-__global__ void __launch_bounds__(128)
-ss_columns_kernel(int axis, int own_implicit, int64_t nx, int64_t ny, int64_t nz,
-                  int64_t n_pencils, const double* __restrict__ dens, const double* __restrict__ xh2,
-                  const double* __restrict__ xco, const int8_t* __restrict__ fam,
-                  const double* __restrict__ ds, double* __restrict__ u_h2,
-                  double* __restrict__ u_co) {
-  int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= n_pencils) return;
-  int64_t base, stride, len;
-  if (axis == 0) { base = p; stride = ny * nz; len = nx; }
-  else if (axis == 1) { int64_t i = p / nz, k = p - i * nz; base = i * ny * nz + k; stride = nz; len = ny; }
-  else { base = p * nz; stride = 1; len = nz; }
-  for (int fwd = 1; fwd >= 0; --fwd) {
-    const int8_t want = (int8_t)(axis * 2 + fwd);
-    double s2 = 0.0, s3 = 0.0;
-    for (int64_t t = 0; t < len; ++t) {
-      int64_t c = base + (fwd ? t : (len - 1 - t)) * stride;
-      double n = dens[c];
-      double l2 = n * xh2[c] * 2.0;
-      double l3 = n * xco[c];
-      if (fam[c] == want) {
-        double dsc = ds[c];
-        u_h2[c] = own_implicit ? dsc * s2 : fmax(dsc * (s2 + 0.5 * l2), 0.0);
-        u_co[c] = fmax(dsc * (s3 + 0.5 * l3), 0.0);
-      }
-      s2 += l2;
-      s3 += l3;
-    }
-  }
-}
-
-// All three axes and both directions in one launch, one thread per
-// (axis, direction, pencil): six times the threads of one axis pass, so
-// every SM holds several warps of independent scans.  Same sums in the same
-// order as ss_columns_kernel.
+// Selected-ray columns (fuv_rt_3d.py:297-392 restricted to each cell's
+// selected ray): for every pencil along an axis and each direction, a
+// running sum of the layers 2 n x_H2 and n x_CO from the illuminated end;
+// cells whose selected ray belongs to that (axis, direction) family take
+// ds x (upstream sum + half their own layer) (with own_implicit the own H2
+// half layer is left out and added inside the chemistry solve).  One launch
+// for all three axes and both directions, one thread per (axis, direction,
+// pencil), so every SM
+// holds several warps of independent scans.
 __global__ void __launch_bounds__(128)
 ss_columns_all_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz,
                       const double* __restrict__ dens, const double* __restrict__ xh2,

@@ -122,8 +122,7 @@ ss_setup_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restrict
 // ds x (upstream sum + half their own layer) (with own_implicit the own H2
 // half layer is left out and added inside the chemistry solve).  One launch
 // for all three axes and both directions, one thread per (axis, direction,
-// pencil), so every SM
-// holds several warps of independent scans.
+// pencil), so every SM holds several warps of independent scans.
 __global__ void __launch_bounds__(128)
 ss_columns_all_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz,
                       const double* __restrict__ dens, const double* __restrict__ xh2,

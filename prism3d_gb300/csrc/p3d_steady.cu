@@ -165,6 +165,7 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   p.h2_implicit = 0;
   for (int k = 0; k < 8; ++k) p.rs[k] = 1.0;
   p.fix_t = 0;
+  p.exact_roots = 0;
   p.quiet_tol = p.quiet_in_tol = p.quiet_b_tol = 0.0;
   p.pe = PeGrid{log_psi_min, log_psi_step, eg_min, eg_step, (int)n_psi, (int)n_eg};
   memcpy(p.lines.cii, cii, sizeof(p.lines.cii));
@@ -494,6 +495,7 @@ int p3d_steady_kernel_times(p3d_steady_t* h, int reps, double* ms4) {
   par.count_thr[0] = par.count_thr[1] = par.count_thr[2] = 1.0;
   par.quiet_tol = 0.0;  // no compaction: every cell solved
   par.quiet_in_tol = 0.0;
+  par.exact_roots = 1;  // the path whose FP64 work the roofline counts
   par.quiet_b_tol = 0.0;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);

@@ -56,6 +56,7 @@ struct SteadyParams {
   // CR-induced CO dissociation, C + OH -> CO
   double rs[8];
   int fix_t;  // 1: T_gas is held at its current value (no thermal balance)
+  int exact_roots;  // 1: mixed thermal roots to therm_tol_mixed even while a cell moves
   PeGrid pe;
   LineParams lines;
 };

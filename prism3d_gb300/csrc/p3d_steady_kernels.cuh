@@ -448,9 +448,16 @@ ss_thermal_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
       delta = fmax(delta, fabs(b_dop - d.b_last[i]) / b_dop);
       int node = d.bis_node[i];
       float margin = d.bis_margin[i];
+      // inexact roots while the cell is still moving: the root tolerance
+      // follows 1% of its last relative change (at most 1e-4), back to
+      // therm_tol_mixed as it settles; a cell's first solve is exact
+      const double cl = d.chg_last[i];
+      const double rtol_t = (isfinite(cl) && !p.exact_roots)
+                                ? fmax(p.therm_tol_mixed, fmin(1e-4, 0.01 * cl))
+                                : p.therm_tol_mixed;
       troot = root_mixed(c, p.lines, c_co_ss, p.theta2, c_lines32, c_co32, g_bisect_mid,
-                         p.therm_tol_mixed, p.therm_max_iter, d.t_root[i], delta, &node, &margin,
-                         &tst, &nev);
+                         rtol_t, p.therm_max_iter, d.t_root[i], delta, &node, &margin, &tst,
+                         &nev);
       d.bis_node[i] = (int16_t)node;
       d.bis_margin[i] = margin;
     } else {

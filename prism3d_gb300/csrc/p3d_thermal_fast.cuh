@@ -344,7 +344,7 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LinePara
     }
     double tn = t - f / slope;
     if (!(slope < 0.0 && tn > t_lo && tn < t_hi)) break;
-    bool small = fabs(tn - t) <= 1e-8 * t;
+    bool small = fabs(tn - t) <= fmax(1e-8, tol) * t;
     t = tn;
     if (small) {
       *status = 0;

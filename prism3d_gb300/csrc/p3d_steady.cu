@@ -315,9 +315,9 @@ int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, in
   par.count_thr[2] = tol * 0.01;
   par.quiet_tol = tol * 0.01;
   par.quiet_in_tol = tol * 0.1;
-  // b ~ sqrt(mean T); a cell's state moves by at most ~ its relative change,
-  // so drift below tol leaves it within the tolerance of its fixed point
-  par.quiet_b_tol = tol;
+  // the Doppler width reaches a cell only through f_H2: held to the columns'
+  // tolerance
+  par.quiet_b_tol = tol * 0.1;
   auto conv = [&](const double* hrow) {
     return hrow[0] < tol || (double)hrow[4] <= (double)n_allow;
   };

@@ -49,7 +49,7 @@ struct SteadyParams {
   double count_thr[3];  // thresholds of the n_gt counters
   double quiet_tol;     // mixed path: skip cells whose last change was <= this
   double quiet_in_tol;  // ... and whose columns moved <= this since
-  double quiet_b_tol;   // ... and whose Doppler width moved <= this since
+  double quiet_b_tol;   // ... and whose H2 shielding factor moved <= this since
   // multipliers of the reduced network's rate coefficients (1 = the
   // reference's): H2 formation, H2 photodissociation, H2 cosmic-ray
   // destruction, C photoionisation, C+ recombination, CO photodissociation,

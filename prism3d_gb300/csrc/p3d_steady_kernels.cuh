@@ -274,12 +274,16 @@ __device__ __forceinline__ double t_update(double t_in, double G, double w_t, do
 // ------------------------------------------------------------ worklist
 // A cell is solved this iteration unless (mixed path, from the fourth
 // iteration on) its last solve changed it by <= quiet_tol and its inputs
-// have moved little since: its selected-ray columns by <= quiet_in_tol, the
-// Doppler width (set by the grid-mean T, which drifts slowly while the last
-// cells settle) by <= quiet_b_tol.  Then it is at its fixed point to about
-// the tolerance and keeps its state.  Solved
-// cells are appended to a dense list (one atomic per warp), so the chemistry
-// and thermal kernels run full warps of active cells.
+// have moved little since: its selected-ray columns by <= quiet_in_tol, and
+// its H2 self-shielding factor by <= quiet_b_tol.  The factor is the one
+// input the Doppler width b (set by the grid-mean T, which drifts while the
+// last cells settle) reaches: it is compared at the cell's current column
+// for b now and b at the last solve, so a drift of the mean T wakes only the
+// cells in the H2 transition, where f_H2 depends on b (not those where it
+// is ~1 or set by its damping-wing term).  Then the cell is at its fixed
+// point to about the tolerance and keeps its state.  Solved cells are
+// appended to a dense list (one atomic per warp), so the chemistry and
+// thermal kernels run full warps of active cells.
 template <bool MIXED>
 __global__ void __launch_bounds__(kThreads)
 ss_mark_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
@@ -295,9 +299,20 @@ ss_mark_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
       const double q = p.quiet_tol, qi = p.quiet_in_tol;
       const double uh2 = d.u_h2[i], uco = d.u_co[i];
       if (d.chg_last[i] <= q && fabs(uh2 - d.u_h2_last[i]) <= qi * fabs(uh2) &&
-          fabs(uco - d.u_co_last[i]) <= qi * fabs(uco) &&
-          fabs(b_dop - d.b_last[i]) <= p.quiet_b_tol * b_dop)
-        active = false;
+          fabs(uco - d.u_co_last[i]) <= qi * fabs(uco)) {
+        const double b_last = d.b_last[i];
+        bool quiet = b_last == b_dop;
+        if (!quiet) {
+          // the column the chemistry's shielding factor sees (chem_prepare /
+          // chem5_eval)
+          const double nh2 = p.h2_implicit ? uh2 + d.ds[i] * d.dens[i] * d.x_h2[i] : uh2;
+          double dfdn;
+          const double f_now = fsh_h2(nh2, b_dop, &dfdn);
+          const double f_last = fsh_h2(nh2, b_last, &dfdn);
+          quiet = fabs(f_now - f_last) <= p.quiet_b_tol * f_now;
+        }
+        if (quiet) active = false;
+      }
     }
     const unsigned m = __ballot_sync(0xffffffffu, active);
     if (m) {

@@ -183,7 +183,7 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   d.dens = s->dens;
   if ((rc = s->alloc(&d.ray, n)) || (rc = s->alloc(&d.fam, n)) || (rc = s->alloc(&d.flags, n)) ||
       (rc = s->alloc(&d.list, n)) || (rc = s->alloc(&d.bis_node, n)) ||
-      (rc = s->alloc(&d.bis_margin, n))) {
+      (rc = s->alloc(&d.bis_margin, n)) || (rc = s->alloc(&d.fh2_slope, n))) {
     delete h;
     return rc;
   }

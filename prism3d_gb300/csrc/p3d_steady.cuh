@@ -36,6 +36,9 @@ struct SteadyDev {
   // ten decisions as bits) and its smallest certified margin |net| / sum|terms|
   int16_t* bis_node;
   float* bis_margin;
+  // |d ln f_H2 / d ln b| at the last chemistry solve (the worklist's test of
+  // a Doppler-width drift)
+  float* fh2_slope;
 };
 
 struct SteadyParams {

@@ -112,6 +112,7 @@ ss_setup_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restrict
     d.flags[i] = 0;
     d.bis_node[i] = 0;
     d.bis_margin[i] = 0.0f;
+    d.fh2_slope[i] = INFINITY;
   }
 }
 
@@ -277,11 +278,11 @@ __device__ __forceinline__ double t_update(double t_in, double G, double w_t, do
 // have moved little since: its selected-ray columns by <= quiet_in_tol, and
 // its H2 self-shielding factor by <= quiet_b_tol.  The factor is the one
 // input the Doppler width b (set by the grid-mean T, which drifts while the
-// last cells settle) reaches: it is compared at the cell's current column
-// for b now and b at the last solve, so a drift of the mean T wakes only the
-// cells in the H2 transition, where f_H2 depends on b (not those where it
-// is ~1 or set by its damping-wing term).  Then the cell is at its fixed
-// point to about the tolerance and keeps its state.  Solved cells are
+// last cells settle) reaches; its relative change is |db / b| times the
+// slope |d ln f_H2 / d ln b| kept from the last solve, so a drift of the mean
+// T wakes only the cells in the H2 transition, where f_H2 depends on b (not
+// those where it is ~1 or set by its damping-wing term).  Then the cell is
+// at its fixed point to about the tolerance and keeps its state.  Solved cells are
 // appended to a dense list (one atomic per warp), so the chemistry and
 // thermal kernels run full warps of active cells.
 template <bool MIXED>
@@ -301,17 +302,9 @@ ss_mark_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
       if (d.chg_last[i] <= q && fabs(uh2 - d.u_h2_last[i]) <= qi * fabs(uh2) &&
           fabs(uco - d.u_co_last[i]) <= qi * fabs(uco)) {
         const double b_last = d.b_last[i];
-        bool quiet = b_last == b_dop;
-        if (!quiet) {
-          // the column the chemistry's shielding factor sees (chem_prepare /
-          // chem5_eval)
-          const double nh2 = p.h2_implicit ? uh2 + d.ds[i] * d.dens[i] * d.x_h2[i] : uh2;
-          double dfdn;
-          const double f_now = fsh_h2(nh2, b_dop, &dfdn);
-          const double f_last = fsh_h2(nh2, b_last, &dfdn);
-          quiet = fabs(f_now - f_last) <= p.quiet_b_tol * f_now;
-        }
-        if (quiet) active = false;
+        if (b_last == b_dop ||
+            fabs(b_dop - b_last) * (double)d.fh2_slope[i] <= p.quiet_b_tol * b_dop)
+          active = false;
       }
     }
     const unsigned m = __ballot_sync(0xffffffffu, active);
@@ -393,6 +386,13 @@ ss_chem_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g,
     d.x_o[i] = fmax(p.x_o_total - y[4], 1e-30);
     d.x_e[i] = fmax(y[2] + p.x_hcop, 1e-30);
     d.fh2[i] = fh2;
+    {  // f_H2 = 0.965 / q^2 + (damping wing), q = 1 + x / b (fsh_h2), never clamped
+       // (0 < f < 0.99997): d ln f / d ln b = 2 (0.965 / q^2) (x / b) / (q f)
+      const double nh2 = cc.ds > 0.0 ? cc.u_h2 + cc.ds * nh * y[1] : cc.u_h2;
+      const double xb = nh2 / 5.0e14 / b_dop;
+      const double q = 1.0 + xb;
+      d.fh2_slope[i] = (float)(2.0 * 0.965 * xb / (q * q * q * fmax(fh2, 1e-300)));
+    }
     d.gamma_pe[i] = gpe;
     d.t_dust[i] = td;
     d.rh2_cell[i] = rh2;

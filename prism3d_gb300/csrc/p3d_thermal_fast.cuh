@@ -313,6 +313,23 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LinePara
   double t;
   if (t_warm > t_lo && t_warm < t_hi) {
     t = t_warm;
+    // a root pinned at an end of [10, 1e5] K (the net heating keeps one
+    // sign over the whole range, every decision went that way): a warm start
+    // within tol of that end that keeps the sign leaves the root between the
+    // end and t -- one FP64 evaluation instead of the polish below
+    const bool at_lo = t_lo == 10.0 && t <= 10.0 * (1.0 + tol);
+    const bool at_hi = t_hi == 1e5 && t >= 1e5 * (1.0 - tol);
+    if (at_lo || at_hi) {
+      const double f = net_heating_fast64(t, c, lp, co, theta2);
+      ++evals;
+      if (at_lo ? !(f > 0.0) : (f > 0.0)) {
+        *status = 0;
+        *n64 = evals;
+        return t;
+      }
+      if (f > 0.0) t_lo = t; else t_hi = t;
+      t = sqrt(t_lo * t_hi);
+    }
   } else {
     t = sqrt(t_lo * t_hi);
     for (int k = 0; k < 4; ++k) {  // FP32 Newton inside the bracket

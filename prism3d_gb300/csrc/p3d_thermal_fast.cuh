@@ -255,17 +255,71 @@ __device__ __forceinline__ double root_plain(const ThermalCtx& c, const LinePara
 // come from `mid_tab`, the FP64 bisection tree: node k has children 2k, 2k+1;
 // a sign is taken from the FP32 evaluation when certified, else from FP64),
 // so the bracket equals the plain path's.  Start: the previous root when it
-// lies in the bracket (warm start), else a few FP32 Newton steps.  Finish:
-// up to three FP64 Newton steps with the FP32 central-difference slope
-// (step 1e-3 T, relative error ~1e-3), done once a step stays in the bracket
-// and moves T by at most 1e-8 T (the slope error then bounds the remaining
-// error by ~1e-11 T); else a two-point FP64 check for a jump of the net
-// heating at T, else the safeguarded FP64 iteration of root_plain to tol.
+// lies in the bracket (warm start; a root pinned at 10 K or 1e5 K is then
+// confirmed by one FP64 evaluation), else a few FP32 Newton steps.  A
+// discontinuity of the net heating within 1e-3 T is tested for a sign change
+// across it (two FP64 evaluations; the root is then the discontinuity).
+// Finish: up to three FP64 Newton steps with the FP32 slope of T's
+// continuous piece (slope32; relative error ~1e-3), done once a step stays
+// in the bracket and moves T by at most 1e-8 T (the slope error then bounds
+// the remaining error by ~1e-11 T); else a two-point FP64 check for a jump
+// of the net heating at T, else the safeguarded FP64 iteration of
+// root_plain to tol.
 // A warm cell replays the last full bisection's decisions when its inputs
 // moved by less than margin / kReuseFactor (relative): the net heating's terms
 // then change by far less than the smallest certified |net| of those
 // decisions.
 constexpr double kReuseFactor = 300.0;
+
+// Discontinuities of the net heating nearest to t from below (<= t; 0 when
+// none) and above (> t; infinity when none): H2 cooling from 100 K,
+// Ly-alpha from 3000 K, CO level J from T_u(J) / 5 (the ladder's break
+// T_u >= 5 T).  T_u(J) = (T_u(1) / 2) J (J + 1): the breaks next to t are
+// those of the J around the real solution of J (J + 1) = 10 t / T_u(1).
+__device__ __forceinline__ void jumps_around(double t, const CoLevel* __restrict__ co,
+                                             double theta2, double* below, double* above) {
+  double lo = 0.0, hi = INFINITY;
+  if (100.0 <= t) lo = 100.0; else hi = 100.0;
+  if (3000.0 <= t) lo = 3000.0; else hi = fmin(hi, 3000.0);
+  const double j = 0.5 * (sqrt(1.0 + 40.0 * t / theta2) - 1.0);
+  const int k0 = (int)fmin(fmax(j, 0.0), 40.0);  // co[k] is J = k + 1
+#pragma unroll
+  for (int dk = -2; dk <= 1; ++dk) {
+    const int k = k0 + dk;
+    if (k >= 0 && k < 40) {
+      const double d = 0.2 * co[k].t_u;
+      if (d <= t) lo = fmax(lo, d); else hi = fmin(hi, d);
+    }
+  }
+  *below = lo;
+  *above = hi;
+}
+
+// Slope of the FP32 twin (net / Gamma_fixed) at t by a difference inside
+// t's continuous piece: a difference across a jump returns the jump's size
+// over the step, and Newton then stalls short of a root next to the jump.
+// Central with half-step 1e-3 t, cut to half the room to the nearest
+// discontinuity; one-sided into the wider side (step <= 1e-3 t) when t sits
+// within 4e-4 t of one.
+__device__ __forceinline__ double slope32(double t, const ThermalCtx32& f32,
+                                          const float* __restrict__ lines32,
+                                          const float* __restrict__ co32,
+                                          const CoLevel* __restrict__ co, double theta2) {
+  double d_lo, d_hi;
+  jumps_around(t, co, theta2, &d_lo, &d_hi);
+  const double r_lo = t - d_lo, r_hi = d_hi - t;
+  float S1, S2;
+  const double room = fmin(r_lo, r_hi);
+  if (room >= 4e-4 * t) {
+    const double h = fmin(1e-3 * t, 0.5 * room);
+    return (double)(net_heating32(t + h, f32, lines32, co32, co, &S1) -
+                    net_heating32(t - h, f32, lines32, co32, co, &S2)) / (2.0 * h);
+  }
+  const double h = fmin(1e-3 * t, 0.5 * fmax(r_lo, r_hi));
+  const float f0 = net_heating32(t, f32, lines32, co32, co, &S1);
+  if (r_hi >= r_lo) return (double)(net_heating32(t + h, f32, lines32, co32, co, &S2) - f0) / h;
+  return (double)(f0 - net_heating32(t - h, f32, lines32, co32, co, &S2)) / h;
+}
 
 __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LineParams& lp,
                                              const CoLevel* __restrict__ co, double theta2,
@@ -311,7 +365,9 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LinePara
     *margin_io = margin == margin ? margin : 0.0f;
   }
   double t;
-  if (t_warm > t_lo && t_warm < t_hi) {
+  // (closed: a root returned on a discontinuity can be a bracket end, e.g.
+  // 100 K, a node of the bisection tree)
+  if (t_warm >= t_lo && t_warm <= t_hi) {
     t = t_warm;
     // a root pinned at an end of [10, 1e5] K (the net heating keeps one
     // sign over the whole range, every decision went that way): a warm start
@@ -333,22 +389,38 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LinePara
   } else {
     t = sqrt(t_lo * t_hi);
     for (int k = 0; k < 4; ++k) {  // FP32 Newton inside the bracket
-      float S, S1, S2;
-      double h = 1e-3 * t;
-      float v = net_heating32(t, f32, lines32, co32, co, &S);
-      float d = (net_heating32(t + h, f32, lines32, co32, co, &S1) -
-                 net_heating32(t - h, f32, lines32, co32, co, &S2)) / (float)(2.0 * h);
-      double tn = t - (double)(v / d);
+      float S;
+      const float v = net_heating32(t, f32, lines32, co32, co, &S);
+      const double d = slope32(t, f32, lines32, co32, co, theta2);
+      double tn = t - (double)v / d;
       if (!(tn > t_lo && tn < t_hi)) break;
       bool small = fabs(tn - t) <= 1e-6 * t;
       t = tn;
       if (small) break;
     }
   }
-  float S1, S2;
-  double h = 1e-3 * t;
-  double slope = (double)(net_heating32(t + h, f32, lines32, co32, co, &S1) -
-                          net_heating32(t - h, f32, lines32, co32, co, &S2)) / (2.0 * h) / K;
+  {  // a root on a discontinuity next to t: sign change across it
+    double d_lo, d_hi;
+    jumps_around(t, co, theta2, &d_lo, &d_hi);
+    const double d = (t - d_lo <= d_hi - t) ? d_lo : d_hi;
+    if (fabs(t - d) <= 1e-3 * t && d >= t_lo && d <= t_hi) {
+      const double a = d * (1.0 - 0.5 * tol), b = d * (1.0 + 0.5 * tol);
+      const double fa = net_heating_fast64(a, c, lp, co, theta2);
+      const double fb = net_heating_fast64(b, c, lp, co, theta2);
+      evals += 2;
+      if (fa > 0.0 && !(fb > 0.0)) {
+        *status = 0;
+        *n64 = evals;
+        return d;
+      }
+      double lo2 = t_lo, hi2 = t_hi;
+      if (fa > 0.0) lo2 = fmax(lo2, a); else hi2 = fmin(hi2, a);
+      if (fb > 0.0) lo2 = fmax(lo2, b); else hi2 = fmin(hi2, b);
+      if (lo2 < hi2) { t_lo = lo2; t_hi = hi2; }
+    }
+  }
+  if (!(t > t_lo && t < t_hi)) t = sqrt(t_lo * t_hi);
+  const double slope = slope32(t, f32, lines32, co32, co, theta2) / K;
   *status = 1;
   for (int k = 0; k < 3; ++k) {  // up to three FP64 Newton steps
     double f = net_heating_fast64(t, c, lp, co, theta2);

@@ -1,0 +1,143 @@
+"""The steady driver's mixed thermal root, built for the host, against its
+plain FP64 root on the oracle's thermal contexts (no GPU).
+
+tests/host_root.cpp compiles prism3d_gb300/csrc/p3d_thermal_fast.cuh with
+g++; the contexts are those of the oracle's steady method on a 24^3 cut of
+the Orion-Bar-like slab (oracle.map_residual of its states after 5 and 6
+outer iterations).  Checked: the mixed root's bracket decisions and polish
+land on the plain root (cold start); a warm start with replayed decisions
+returns a sign change of the net heating (or a root pinned at 10 K / 1e5 K,
+which then costs one FP64 evaluation); the warm and cold roots agree.  The
+device build of the same source runs these paths in the -m gpu tests.
+"""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+TOL = 1e-10  # the mixed path's settled root tolerance
+
+
+def _cuda_include():
+    for d in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if d and os.path.exists(os.path.join(d, "include", "cuda_runtime.h")):
+            return os.path.join(d, "include")
+    return None
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    cxx = shutil.which("g++")
+    inc = _cuda_include()
+    if not cxx or not inc:
+        pytest.skip("needs g++ and the CUDA headers")
+    out = str(tmp_path_factory.mktemp("hostroot") / "libhostroot.so")
+    src = os.path.join(ROOT, "tests", "host_root.cpp")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", inc, src, "-o", out],
+                   check=True, capture_output=True)
+    L = ctypes.CDLL(out)
+    from prism3d_gb300 import tables
+    lp = [np.ascontiguousarray(a, dtype=np.float64) for a in tables.line_params()]
+    co = np.ascontiguousarray(tables.co_ladder(), dtype=np.float64)
+    L.hr_init(*[a.ctypes.data_as(ctypes.c_void_p) for a in lp], co.ctypes.data_as(ctypes.c_void_p))
+    return L
+
+
+@pytest.fixture(scope="module")
+def contexts():
+    from prism3d_gb300 import fields
+    from prism3d_gb300.core import directional_G0
+    dens = fields.orion_bar_slab(24, seed=1)
+    g0 = directional_G0(2.6e4, [-1.0, 0.0, 0.0], 2)
+    keep = {}
+    keys = ("x_HI", "x_H2", "x_Cp", "x_C", "x_CO", "x_O", "x_e", "T_gas")
+
+    def cb(it, st):
+        if it in (5, 6):
+            keep[it] = {k: st[k].copy() for k in keys}
+    O.steady_run(dens, g0, fields.CELL_CM, nside=2, zeta0=2e-16, T_init=100.0, max_outer=7,
+                 tol=1e-300, w_chem=0.1, callback=cb)
+    out = []
+    for it in (5, 6):
+        _, _, _, ctx = O.map_residual(keep[it], dens, g0, fields.CELL_CM, 2, 2e-16)
+        out.append(np.ascontiguousarray(np.stack([np.ravel(c) for c in ctx], axis=1)))
+    return out
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _mixed(L, ctx, t_warm, delta, node, margin, tol=TOL):
+    n = ctx.shape[0]
+    t = np.zeros(n)
+    ev = np.zeros(n, np.int32)
+    st = np.zeros(n, np.int32)
+    L.hr_root_mixed(ctypes.c_long(n), _p(ctx), _p(np.ascontiguousarray(t_warm, dtype=np.float64)),
+                    _p(np.ascontiguousarray(delta, dtype=np.float64)), _p(node), _p(margin),
+                    ctypes.c_double(tol), _p(t), _p(ev), _p(st))
+    return t, ev, st
+
+
+def _plain(L, ctx):
+    n = ctx.shape[0]
+    t = np.zeros(n)
+    ev = np.zeros(n, np.int32)
+    st = np.zeros(n, np.int32)
+    L.hr_root_plain(ctypes.c_long(n), _p(ctx), ctypes.c_double(1e-12), _p(t), _p(ev), _p(st))
+    return t, ev, st
+
+
+def _net(L, ctx, t):
+    out = np.zeros(ctx.shape[0])
+    L.hr_net64(ctypes.c_long(ctx.shape[0]), _p(ctx), _p(np.ascontiguousarray(t)), _p(out))
+    return out
+
+
+def test_cold_mixed_root_matches_plain(lib, contexts):
+    ctx = contexts[1]
+    n = ctx.shape[0]
+    tp, _, sp = _plain(lib, ctx)
+    node, margin = np.zeros(n, np.int32), np.zeros(n, np.float32)
+    tm, ev, sm = _mixed(lib, ctx, np.zeros(n), np.full(n, np.inf), node, margin)
+    assert sp.sum() == 0 and sm.sum() == 0
+    rel = np.abs(tm - tp) / tp
+    assert np.mean(rel <= 1e-6) >= 0.999, np.sort(rel)[-10:]
+    # every full bisection left a node of the tree's last level
+    assert np.all((node >= 1024) & (node < 2048))
+
+
+def test_warm_root_is_a_sign_change_and_pinned_roots_cost_one_evaluation(lib, contexts):
+    c5, c6 = contexts
+    n = c5.shape[0]
+    node, margin = np.zeros(n, np.int32), np.zeros(n, np.float32)
+    t5, _, _ = _mixed(lib, c5, np.zeros(n), np.full(n, np.inf), node, margin)
+    delta = np.max(np.abs(c6 - c5) / np.maximum(np.abs(c6), 1e-300), axis=1)
+    tw, ev, st = _mixed(lib, c6, t5, delta, node, margin)
+    assert st.sum() == 0
+    lo_pin = tw <= 10.0 * (1.0 + 2 * TOL)
+    hi_pin = tw >= 1e5 * (1.0 - 2 * TOL)
+    inner = ~(lo_pin | hi_pin)
+    assert lo_pin.any(), "the slab cut should hold cells at the 10 K floor"
+    # pinned: the net heating keeps its sign at the root; one FP64 evaluation
+    assert np.all(_net(lib, c6[lo_pin], tw[lo_pin]) <= 0.0)
+    assert np.all(_net(lib, c6[hi_pin], tw[hi_pin]) > 0.0)
+    warm_pinned = lo_pin & (t5 <= 10.0 * (1.0 + TOL))
+    assert warm_pinned.any() and np.all(ev[warm_pinned] == 1), np.bincount(ev[warm_pinned])
+    # elsewhere the root brackets a sign change within 1e-7 T
+    fa = _net(lib, c6[inner], tw[inner] * (1.0 - 1e-7))
+    fb = _net(lib, c6[inner], tw[inner] * (1.0 + 1e-7))
+    assert np.all((fa > 0.0) & (fb <= 0.0))
+    # warm and cold starts agree (a bracket holding two sign changes may let
+    # them pick different ones: allowed for a handful of cells)
+    nc, mc = np.zeros(n, np.int32), np.zeros(n, np.float32)
+    tc, evc, _ = _mixed(lib, c6, np.zeros(n), np.full(n, np.inf), nc, mc)
+    rel = np.abs(tw - tc) / tc
+    assert np.mean(rel <= 1e-6) >= 0.99, np.sort(rel)[-10:]
+    assert ev.mean() < evc.mean()

@@ -1,0 +1,123 @@
+"""The steady driver's per-cell chemistry, built for the host, against the
+oracle's FP64 restatement of the method (no GPU).
+
+tests/host_chem.cpp compiles prism3d_gb300/csrc/p3d_newton.cuh with g++.
+The inputs are those the oracle's steady method hands its chemistry solve
+(oracle.chem_steady) in outer iterations 0 and 5 on a 24^3 cut of the
+Orion-Bar-like slab: rates, shielding columns, Doppler width and the start
+abundances.  Both builds converge to the oracle's steady state (the
+mixed one factorises in FP32 but iterates on FP64 residuals to the same
+rtol 1e-12): measured ~1e-15, asserted 1e-12 (FP64) and 1e-10 (mixed) for
+every species above 1e-20 of n_H.
+The device build of the same source runs in the -m gpu tests.
+"""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SPECIES = ("x_HI", "x_H2", "x_Cp", "x_C", "x_CO")
+
+
+def _cuda_include():
+    for d in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if d and os.path.exists(os.path.join(d, "include", "cuda_runtime.h")):
+            return os.path.join(d, "include")
+    return None
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    cxx = shutil.which("g++")
+    inc = _cuda_include()
+    if not cxx or not inc:
+        pytest.skip("needs g++ and the CUDA headers")
+    out = str(tmp_path_factory.mktemp("hostchem") / "libhostchem.so")
+    src = os.path.join(ROOT, "tests", "host_chem.cpp")
+    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", inc, src, "-o", out],
+                   check=True, capture_output=True)
+    return ctypes.CDLL(out)
+
+
+@pytest.fixture(scope="module")
+def calls(monkeypatch_module):
+    """(inputs, oracle outputs) of the oracle's chemistry solve at outer
+    iterations 0 and 5."""
+    from prism3d_gb300 import fields
+    from prism3d_gb300.core import directional_G0
+    dens = fields.orion_bar_slab(24, seed=1)
+    g0 = directional_G0(2.6e4, [-1.0, 0.0, 0.0], 2)
+    seen = []
+    real = O.chem_steady
+
+    def spy(*args, **kw):
+        k = len(seen)
+        keep = k in (0, 5)
+        inp = [np.array(a, dtype=np.float64, copy=True) if isinstance(a, np.ndarray) else a
+               for a in args] if keep else None
+        out = real(*args, **kw)
+        if keep:
+            res = [np.array(a, copy=True) for a in args[8:15]]
+            seen.append((inp, dict(kw), res, out))
+        else:
+            seen.append(None)
+        return out
+    monkeypatch_module.setattr(O, "chem_steady", spy)
+    O.steady_run(dens, g0, fields.CELL_CM, nside=2, zeta0=2e-16, T_init=100.0, max_outer=6,
+                 tol=1e-300, w_chem=0.1)
+    return [c for c in seen if c is not None]
+
+
+@pytest.fixture(scope="module")
+def monkeypatch_module():
+    mp = pytest.MonkeyPatch()
+    yield mp
+    mp.undo()
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _host_solve(L, inp, kw, mixed):
+    (n_h, kpd0, kci, acp, kco0, rh2, rcr, x_c_total, x_hi, x_h2, x_cp, x_c, x_co, _x_o, _x_e,
+     x_hcop) = inp
+    kco_cr, u_h2, u_co, _ds, b_dop = kw["selfshield"]
+    hcop = np.ravel(x_hcop)
+    assert np.all(hcop == hcop[0])  # the driver takes one x_HCO+
+    n = np.ravel(n_h).size
+    y = np.ascontiguousarray(np.stack([np.ravel(a) for a in (x_hi, x_h2, x_cp, x_c, x_co)],
+                                      axis=1))
+    f64 = [np.ascontiguousarray(np.ravel(a), dtype=np.float64) for a in
+           (n_h, kpd0, kci, acp, kco0, rh2, rcr)]
+    ss = [np.ascontiguousarray(np.ravel(a), dtype=np.float64) for a in (kco_cr, u_h2, u_co)]
+    fh2 = np.zeros(n)
+    it = np.zeros(n, np.int32)
+    st = np.zeros(n, np.int32)
+    L.hc_chem_steady(ctypes.c_long(n), *[_p(a) for a in f64], ctypes.c_double(x_c_total),
+                     ctypes.c_double(hcop[0]), *[_p(a) for a in ss], ctypes.c_double(b_dop),
+                     ctypes.c_int(int(mixed)), ctypes.c_int(kw.get("max_iter", 200)),
+                     ctypes.c_double(kw.get("rtol", 1e-12)), _p(y), _p(fh2), _p(it), _p(st))
+    return y, fh2, st
+
+
+@pytest.mark.parametrize("mixed,tol", [(False, 1e-12), (True, 1e-10)])
+def test_host_chemistry_matches_oracle(lib, calls, mixed, tol):
+    assert len(calls) == 2
+    for inp, kw, res, (_, _, status, fsh) in calls:
+        assert not kw.get("h2_implicit") and not kw.get("co_implicit")
+        y, fh2, st = _host_solve(lib, inp, kw, mixed)
+        ok = (st == 0) & (np.ravel(status) == 0)
+        assert ok.mean() > 0.999, (int((st != 0).sum()), int((np.ravel(status) != 0).sum()))
+        for c, name in enumerate(SPECIES):
+            ref = np.ravel(res[c])
+            m = ok & (ref > 1e-20)
+            rel = np.abs(y[:, c] - ref)[m] / ref[m]
+            assert rel.max() <= tol, (name, mixed, rel.max())
+        np.testing.assert_allclose(fh2[ok], fsh[0][ok], rtol=max(tol, 1e-12))

@@ -7,8 +7,10 @@ the Orion-Bar-like slab (oracle.map_residual of its states after 5 and 6
 outer iterations).  Checked: the mixed root's bracket decisions and polish
 land on the plain root (cold start); a warm start with replayed decisions
 returns a sign change of the net heating (or a root pinned at 10 K / 1e5 K,
-which then costs one FP64 evaluation); the warm and cold roots agree.  The
-device build of the same source runs these paths in the -m gpu tests.
+which then costs one FP64 evaluation); the warm and cold roots agree; and
+the oracle's whole steady method, run with the mixed root in place of its
+plain one, reaches the plain fixed point to 1e-6 in every cell.  The device
+build of the same source runs these paths in the -m gpu tests.
 """
 import ctypes
 import os
@@ -141,3 +143,48 @@ def test_warm_root_is_a_sign_change_and_pinned_roots_cost_one_evaluation(lib, co
     rel = np.abs(tw - tc) / tc
     assert np.mean(rel <= 1e-6) >= 0.99, np.sort(rel)[-10:]
     assert ev.mean() < evc.mean()
+
+
+def test_mixed_root_in_the_outer_loop_reaches_the_plain_fixed_point(lib, monkeypatch):
+    """The oracle's steady method on the 24^3 slab cut, once with its plain
+    FP64 roots and once with the host-built mixed root in their place (warm
+    starts, replayed decisions and the one-evaluation pinned roots across
+    outer iterations, tol 1e-10): same iteration count, and every cell's T
+    and abundances within 1e-6 of the plain fixed point.  (The root before
+    its Newton slope was confined to T's continuous piece left 20 cells of
+    this grid 1e-6 to 9e-3 away.)"""
+    from prism3d_gb300 import fields
+    from prism3d_gb300.core import directional_G0
+    dens = fields.orion_bar_slab(24, seed=1)
+    g0 = directional_G0(2.6e4, [-1.0, 0.0, 0.0], 2)
+    keys = ("T_gas", "x_HI", "x_H2", "x_Cp", "x_C", "x_CO")
+
+    def solve():
+        st, hist = O.steady_run(dens, g0, fields.CELL_CM, nside=2, zeta0=2e-16, T_init=100.0,
+                                max_outer=600, tol=1e-8, w_chem=0.1)
+        return {k: st[k].ravel().copy() for k in keys}, len(hist), hist[-1]["dmax"]
+
+    plain, it_p, d_p = solve()
+    state = {}
+
+    def mixed_root(ctx10, *args, **kw):
+        c = np.ascontiguousarray(np.stack([np.ravel(np.asarray(x, dtype=np.float64))
+                                           for x in ctx10], axis=1))
+        n = c.shape[0]
+        if not state:
+            state.update(t=np.zeros(n), node=np.zeros(n, np.int32),
+                         margin=np.zeros(n, np.float32), ctx=None)
+        delta = (np.full(n, np.inf) if state["ctx"] is None else
+                 np.max(np.abs(c - state["ctx"]) / np.maximum(np.abs(c), 1e-300), axis=1))
+        t, ev, st = _mixed(lib, c, state["t"], delta, state["node"], state["margin"])
+        state["t"], state["ctx"] = t, c
+        return t, ev.astype(np.int64), st
+
+    monkeypatch.setattr(O, "thermal_root", mixed_root)
+    mixed, it_m, d_m = solve()
+    assert d_p < 1e-8 and d_m < 1e-8
+    assert it_m == it_p
+    for k in keys:
+        m = np.abs(plain[k]) > 1e-20
+        rel = np.abs(mixed[k] - plain[k])[m] / np.abs(plain[k])[m]
+        assert rel.max() <= 1e-6, (k, rel.max(), int((rel > 1e-6).sum()))

@@ -23,6 +23,15 @@ __device__ __forceinline__ double fsh_h2(double n, double b, double* dfdn) {
   return fmin(fmax(f, 0.0), 1.0);
 }
 
+// |d ln f_H2 / d ln b| at column n given f = fsh_h2(n, b): only the
+// 0.965 / q^2 term (q = 1 + x / b) depends on b, and f is never clipped
+// (0 < f < 0.99997), so d ln f / d ln b = 2 (0.965 / q^2) (x / b) / (q f).
+__device__ __forceinline__ double fsh_h2_dlnb(double n, double b, double f) {
+  const double xb = n / 5.0e14 / b;
+  const double q = 1.0 + xb;
+  return 2.0 * 0.965 * xb / (q * q * q * fmax(f, 1e-300));
+}
+
 // f_shield_CO (shielding.py:136-171) and its N_H2 derivative.
 __device__ __forceinline__ double fsh_co(double nco_in, double nh2_in, double* d_h2) {
   double nco = fmax(nco_in, 1.0), nh2 = fmax(nh2_in, 1.0);

@@ -386,13 +386,9 @@ ss_chem_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g,
     d.x_o[i] = fmax(p.x_o_total - y[4], 1e-30);
     d.x_e[i] = fmax(y[2] + p.x_hcop, 1e-30);
     d.fh2[i] = fh2;
-    {  // f_H2 = 0.965 / q^2 + (damping wing), q = 1 + x / b (fsh_h2), never clamped
-       // (0 < f < 0.99997): d ln f / d ln b = 2 (0.965 / q^2) (x / b) / (q f)
-      const double nh2 = cc.ds > 0.0 ? cc.u_h2 + cc.ds * nh * y[1] : cc.u_h2;
-      const double xb = nh2 / 5.0e14 / b_dop;
-      const double q = 1.0 + xb;
-      d.fh2_slope[i] = (float)(2.0 * 0.965 * xb / (q * q * q * fmax(fh2, 1e-300)));
-    }
+    // the column the shielding factor saw (chem_prepare / chem5_eval)
+    const double nh2_sh = cc.ds > 0.0 ? cc.u_h2 + cc.ds * nh * y[1] : cc.u_h2;
+    d.fh2_slope[i] = (float)fsh_h2_dlnb(nh2_sh, b_dop, fh2);
     d.gamma_pe[i] = gpe;
     d.t_dust[i] = td;
     d.rh2_cell[i] = rh2;

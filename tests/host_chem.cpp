@@ -51,3 +51,14 @@ extern "C" void hc_chem_steady(long n, const double* n_h, const double* kpd0,
     iters[i] = it;
   }
 }
+
+// H2 self-shielding factor and the slope the steady driver's worklist keeps
+// (|d ln f_H2 / d ln b|), for the CPU tests.
+extern "C" void hc_fsh_h2(long n, const double* nh2, const double* b, double* f,
+                          double* dlnb) {
+  for (long i = 0; i < n; ++i) {
+    double dfdn;
+    f[i] = fsh_h2(nh2[i], b[i], &dfdn);
+    dlnb[i] = fsh_h2_dlnb(nh2[i], b[i], f[i]);
+  }
+}

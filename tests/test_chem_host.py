@@ -121,3 +121,29 @@ def test_host_chemistry_matches_oracle(lib, calls, mixed, tol):
             rel = np.abs(y[:, c] - ref)[m] / ref[m]
             assert rel.max() <= tol, (name, mixed, rel.max())
         np.testing.assert_allclose(fh2[ok], fsh[0][ok], rtol=max(tol, 1e-12))
+
+
+def test_shielding_slope_in_doppler_width(lib):
+    """The worklist wakes a settled cell when |db / b| x |d ln f_H2 / d ln b|
+    exceeds its tolerance; the kept slope (closed form) against a central
+    difference of f_H2 itself in ln b, and f_H2 against the oracle's
+    f_shield_H2, over 1e12-1e24 cm^-2 and b 0.5-20 km/s."""
+    rng = np.random.default_rng(3)
+    n = 4000
+    nh2 = 10 ** rng.uniform(12, 24, n)
+    b = rng.uniform(0.5, 20.0, n)
+    f = np.zeros(n)
+    s = np.zeros(n)
+    lib.hc_fsh_h2(ctypes.c_long(n), _p(nh2), _p(b), _p(f), _p(s))
+    fp, fm = np.zeros(n), np.zeros(n)
+    h = 1e-5
+    for out, bb in ((fp, b * np.exp(h)), (fm, b * np.exp(-h))):
+        junk = np.zeros(n)
+        lib.hc_fsh_h2(ctypes.c_long(n), _p(nh2), _p(np.ascontiguousarray(bb)), _p(out), _p(junk))
+    fd = (np.log(fp) - np.log(fm)) / (2 * h)
+    assert np.all(s >= 0.0) and s.max() <= 2.0
+    # (atol: the difference quotient's rounding, ~1e-16 / h)
+    np.testing.assert_allclose(s, np.abs(fd), rtol=1e-5, atol=1e-9)
+    # the kernel's f_H2 is the reference's f_shield_H2 with b = sqrt(2 k T / m_H2) / 1e5
+    T = (b * 1e5) ** 2 * O.m_H2 / (2.0 * O.k_boltz)
+    np.testing.assert_allclose(f, O.f_shield_H2(nh2, T), rtol=1e-12)

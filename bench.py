@@ -1,7 +1,7 @@
 """Benchmark: converged cells/sec of the PRISM-3D steady state on one GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload slab128] [--plain-full]
+                    [--workload slab128] [--plain full|estimate|auto]
 
 Workload (default): the 128^3 Orion-Bar-like slab -- n_H rising as a tanh
 ramp from 1e3 to 1e5 cm^-3 along x over ~0.05 pc times a seeded log-normal
@@ -20,9 +20,11 @@ most max(8, 1e-5 n) cells change by more than 1e-8.
              (density and tables host->device) + reset + run + p3d_steady_get
              of the 8 state fields, wall clock.
   plain      the plain FP64 path (same algorithm, FP64 everywhere, no warm
-             starts or compaction, host-checked every iteration): per-
-             iteration time over a bounded sample of iterations, and with
-             --plain-full its own full solve.
+             starts or compaction, host-checked every iteration): its own
+             full solve and the per-species difference of the mixed state
+             from it (--plain full; the default up to 2^21 cells, ~100 s at
+             128^3), or the per-iteration time over a bounded sample of
+             iterations (--plain estimate; the default above 2^21 cells).
   cpu_baseline / --impl reference: the CPU oracle (C restatement of the
              reference's kernels with OpenMP + NumPy ray march) timing one
              reference outer iteration (solver_3d.py:262-376 with the Rust
@@ -189,9 +191,11 @@ def run_gb300(args, ws, rank, local):
     s2.close()
     h2d = dens.nbytes + 8 * (s.tables.pe_table.size + 3 * s.tables.n_bins + 60)
     d2h = sum(a.nbytes for a in outs)
-    # plain FP64 path: bounded sample, or full solve
+    # plain FP64 path: full solve (and the mixed state's difference from it),
+    # or a bounded sample of iterations
     s.reset()
-    if args.plain_full:
+    plain_full = args.plain_full or args.plain == "full" or (args.plain == "auto" and n <= 1 << 21)
+    if plain_full:
         t0 = time.perf_counter()
         okp = s.run(max_iterations=4000, convergence_tol=args.tol, mixed=False, n_allow=n_allow,
                     w_chem=args.w_chem)
@@ -432,7 +436,10 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--w-chem", type=float, default=0.1,
                     help="abundance damping (the reference uses 0.5)")
-    ap.add_argument("--plain-full", action="store_true")
+    ap.add_argument("--plain", default="auto", choices=["auto", "full", "estimate"],
+                    help="plain FP64 comparison: a full solve (auto: up to 2^21 cells) or a "
+                         "per-iteration sample")
+    ap.add_argument("--plain-full", action="store_true", help="same as --plain full")
     ap.add_argument("--plain-iters", type=int, default=20)
     ap.add_argument("--ref-iters", type=int, default=439,
                     help="outer iterations the reference arm is scaled by (the GPU solve of "

@@ -29,6 +29,9 @@
  *                              prism3d/solver_3d.py:573-585)
  *  p3d_solve_thermal_vec      rust/src/thermal.rs:282-360
  *                             (called at prism3d/solver_3d.py:782-796)
+ *  p3d_total_heating_cooling  prism3d/solver_3d.py:898-1050
+ *                             (_total_heating_vec / _total_cooling_vec, the
+ *                              diagnostics Gamma and Lambda, :891-892)
  *  p3d_pe_heating_vec         rust/src/pe_table.rs:43-141
  *                             (called at prism3d/grains/themis_tables.py:191-201)
  *  p3d_version                rust/src/lib.rs:22-26
@@ -110,6 +113,33 @@ int p3d_solve_thermal_vec_dev(int64_t n_cells, const double *gamma_fixed,
                               const double *oi63_params, const double *oi145_params,
                               const double *ci_params, int64_t n_bisect, int64_t n_newton,
                               double *t_gas, void *stream);
+
+/* ---------------------------------------------------------------------
+ * Diagnostics Gamma and Lambda [erg cm^-3 s^-1] at temperatures t
+ * (_total_heating_vec / _total_cooling_vec, prism3d/solver_3d.py:898-1050):
+ * Gamma = gamma_fixed + the signed gas-grain exchange, Lambda = the sum of
+ * the cooling terms the thermal balance subtracts.  Same context and line
+ * parameters as p3d_solve_thermal_vec; in: t [n_cells]; out: gamma_out,
+ * lambda_out [n_cells].
+ * ------------------------------------------------------------------- */
+int p3d_total_heating_cooling(int64_t n_cells, const double *gamma_fixed,
+                              const double *gg_coeff, const double *t_dust, const double *n_e,
+                              const double *n_hi, const double *n_h2, const double *n_co,
+                              const double *n_cp_nh, const double *n_o_nh,
+                              const double *n_c_nh, const double *cii_params,
+                              const double *oi63_params, const double *oi145_params,
+                              const double *ci_params, const double *t, double *gamma_out,
+                              double *lambda_out);
+
+int p3d_total_heating_cooling_dev(int64_t n_cells, const double *gamma_fixed,
+                                  const double *gg_coeff, const double *t_dust,
+                                  const double *n_e, const double *n_hi, const double *n_h2,
+                                  const double *n_co, const double *n_cp_nh,
+                                  const double *n_o_nh, const double *n_c_nh,
+                                  const double *cii_params, const double *oi63_params,
+                                  const double *oi145_params, const double *ci_params,
+                                  const double *t, double *gamma_out, double *lambda_out,
+                                  void *stream);
 
 /* ---------------------------------------------------------------------
  * THEMIS photoelectric heating (rust/src/pe_table.rs:43-141).
@@ -252,6 +282,10 @@ typedef struct p3d_steady p3d_steady_t;
 #define P3D_F_GAMMA_PE 14
 #define P3D_F_ZETA 15
 #define P3D_F_F_SH_H2 16
+/* diagnostics at the current T (solver_3d.py:891-892): total heating and
+ * cooling with the context of each cell's last solve */
+#define P3D_F_GAMMA 17
+#define P3D_F_LAMBDA 18
 
 int p3d_steady_create(p3d_steady_t **out, int64_t nx, int64_t ny, int64_t nz,
                       const double *density, const double *g0_ext, int64_t n_g0,

@@ -27,6 +27,7 @@ from .build_oracle import build as _build
 
 # constants: prism3d/utils/constants.py (CGS)
 k_boltz = 1.380649e-16
+h_planck = 6.62607015e-27
 m_H = 1.6735575e-24
 m_H2 = 2.0 * m_H
 eV_to_erg = 1.602176634e-12
@@ -742,6 +743,62 @@ def map_residual(st_in, density, G0_external, cell_size, nside, zeta0, tables=No
     ctx = thermal_ctx(st2, fsh[0].reshape(shp))
     G, _, _ = thermal_root(ctx, *lines, tol=1e-12)
     return x_star, G.reshape(shp), ray, ctx
+
+
+def total_heating_cooling(ctx10, T, lines=None):
+    """(Gamma, Lambda) [erg cm^-3 s^-1] at T: _total_heating_vec and
+    _total_cooling_vec (solver_3d.py:898-1050) restated on the thermal
+    context (thermal_ctx): Gamma = the fixed heating + the signed gas-grain
+    exchange; Lambda = the cooling terms in the reference's order."""
+    if lines is None:
+        from prism3d_gb300.tables import line_params
+        lines = line_params()
+    cii, oi63, oi145, ci = (np.asarray(a, dtype=np.float64) for a in lines)
+    gf, gg, td, n_e, n_hi, n_h2, n_co, n_cp, n_o, n_c = (np.asarray(a, dtype=np.float64).ravel()
+                                                         for a in ctx10)
+    T = np.asarray(T, dtype=np.float64).ravel()
+    sqrt_t = np.sqrt(T)
+    gamma = gf + gg * sqrt_t * (td - T)
+
+    def level(q, l, x_nh):  # two-level line: l = [freq, A, T_ul, g_u, g_l]
+        r_lu = (l[3] / l[4]) * q * np.exp(-l[2] / T)
+        return x_nh * r_lu / (r_lu + l[1] + q) * l[1] * h_planck * l[0]
+
+    lam = np.zeros_like(T)
+    q = (8.63e-6 / (cii[4] * sqrt_t) * 2.15 * np.exp(-cii[2] / T) * n_e +
+         8.0e-10 * (T / 100.0) ** 0.07 * n_hi + 4.9e-10 * (T / 100.0) ** 0.12 * n_h2)
+    lam += level(q, cii, n_cp)
+    q = 9.2e-12 * T ** 0.67 * n_hi + 4.5e-12 * T ** 0.64 * n_h2 + 1.4e-8 * (T / 100.0) ** 0.39 * n_e
+    lam += level(q, oi63, n_o)
+    q = 4.0e-12 * T ** 0.60 * n_hi + 2.0e-12 * T ** 0.58 * n_h2 + 5.0e-9 * (T / 100.0) ** 0.39 * n_e
+    lam += level(q, oi145, n_o)
+    for l in (ci[:5], ci[5:]):
+        q = (1.0e-10 * (T / 100.0) ** 0.3 * n_hi + 5.0e-11 * (T / 100.0) ** 0.3 * n_h2 +
+             2.0e-7 * (T / 100.0) ** (-0.5) * n_e)
+        lam += level(q, l, n_c)
+    co = co_levels()
+    for k in range(40):  # J_u = k + 1; level included while T_u < 5 T
+        t_u, a_co, g_ratio, j_factor, ahv = co[k]
+        mask = t_u < 5.0 * T
+        if not np.any(mask):
+            break
+        gam = 3.3e-11 * (T / 100.0) ** 0.5 * j_factor
+        r_lu = g_ratio * gam * n_h2 * np.exp(-t_u / T)
+        r_ul = a_co + gam * n_h2
+        lam += np.where(mask, n_co * r_lu / (r_lu + r_ul) * ahv, 0.0)
+    x = np.clip(np.log10(np.maximum(T, 100.0)), 2.0, 4.5)
+    llh = (-24.311 + 3.5692 * x - 11.332 * x ** 2 + 15.738 * x ** 3 - 10.581 * x ** 4 +
+           3.5803 * x ** 5 - 0.48365 * x ** 6)
+    llh2 = (-24.311 + 4.6585 * x - 14.272 * x ** 2 + 19.779 * x ** 3 - 13.255 * x ** 4 +
+            4.4840 * x ** 5 - 0.60504 * x ** 6)
+    l0 = 10.0 ** llh * n_hi + 10.0 ** llh2 * n_h2
+    lte = 10.0 ** (-19.703 + 0.5 * x)
+    lam += np.where(T >= 100.0, n_h2 * l0 * lte / np.maximum(l0 + lte, 1e-50), 0.0)
+    q_lu = 2.41e-6 / sqrt_t * 0.486 * np.exp(-1.18e5 / T)
+    lam += np.where(T >= 3000.0, n_hi * n_e * q_lu * 10.2 * eV_to_erg, 0.0)
+    lam += np.maximum(gg * sqrt_t * (T - td), 0.0)
+    lam += n_cp * n_e * 4.67e-12 * (T / 300.0) ** (-0.6) * k_boltz * T
+    return gamma, lam
 
 
 def net_heating_at(ctx, t, lines=None):

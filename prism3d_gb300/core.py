@@ -133,6 +133,36 @@ def solve_thermal_vec(gamma_fixed, gg_coeff, t_dust, n_e, n_hi, n_h2, n_co, n_cp
                int(n_bisect), int(n_newton), p(t))
 
 
+def total_heating_cooling(gamma_fixed, gg_coeff, t_dust, n_e, n_hi, n_h2, n_co, n_cp_nh, n_o_nh,
+                          n_c_nh, cii_params, oi63_params, oi145_params, ci_params, t,
+                          gamma_out, lambda_out):
+    """Diagnostics Gamma and Lambda [erg cm^-3 s^-1] at temperatures t
+    (_total_heating_vec / _total_cooling_vec, solver_3d.py:898-1050) from the
+    thermal context of solve_thermal_vec; writes gamma_out and lambda_out."""
+    n = _arr("gamma_fixed", gamma_fixed).shape[0]
+    ctx = [gamma_fixed] + [_arr(k, a, n) for k, a in zip(
+        ("gg_coeff", "t_dust", "n_e", "n_hi", "n_h2", "n_co", "n_cp_nh", "n_o_nh", "n_c_nh"),
+        (gg_coeff, t_dust, n_e, n_hi, n_h2, n_co, n_cp_nh, n_o_nh, n_c_nh))]
+    lines = []
+    for k, a, m in (("cii_params", cii_params, 5), ("oi63_params", oi63_params, 5),
+                    ("oi145_params", oi145_params, 5), ("ci_params", ci_params, 10)):
+        a = _arr(k, np.ascontiguousarray(a.cpu().numpy() if _is_torch(a) else a))
+        if a.shape[0] < m:
+            raise ValueError(f"{k}: needs {m} values")
+        lines.append(a)
+    t = _arr("t", t, n)
+    g = _arr("gamma_out", gamma_out, n, True)
+    lam = _arr("lambda_out", lambda_out, n, True)
+    dev, stream = _stream_of([*ctx, t, g, lam])
+    p = L.dptr
+    if dev:
+        L.call("p3d_total_heating_cooling_dev", n, *[p(a) for a in ctx], *[p(a) for a in lines],
+               p(t), p(g), p(lam), stream)
+    else:
+        L.call("p3d_total_heating_cooling", n, *[p(a) for a in ctx], *[p(a) for a in lines],
+               p(t), p(g), p(lam))
+
+
 def pe_heating_vec(pe_table, log_psi_min, log_psi_step, n_psi, eg_min, eg_step, n_eg,
                    bin_sigma_abs, bin_dn_da_da, bin_is_nano, g0, t_gas, x_e, n_h, f_nano, e_g,
                    gamma_pe_out):

@@ -309,6 +309,63 @@ int p3d_solve_thermal_vec(int64_t n, const double* gamma_fixed, const double* gg
   return sync_check(st->stream, "solve_thermal_vec");
 }
 
+int p3d_total_heating_cooling_dev(int64_t n, const double* gamma_fixed, const double* gg_coeff,
+                                  const double* t_dust, const double* n_e, const double* n_hi,
+                                  const double* n_h2, const double* n_co, const double* n_cp_nh,
+                                  const double* n_o_nh, const double* n_c_nh, const double* cii,
+                                  const double* oi63, const double* oi145, const double* ci,
+                                  const double* t, double* gamma_out, double* lambda_out,
+                                  void* stream) {
+  DeviceState* st;
+  int rc = get_state(&st);
+  if (rc) return rc;
+  if (n < 0) return set_error(P3D_EINVAL, "n_cells < 0");
+  if (any_null({cii, oi63, oi145, ci})) return set_error(P3D_EINVAL, "null line parameters");
+  if (n == 0) return P3D_OK;
+  if (any_null({gamma_fixed, gg_coeff, t_dust, n_e, n_hi, n_h2, n_co, n_cp_nh, n_o_nh, n_c_nh,
+                t, gamma_out, lambda_out}))
+    return set_error(P3D_EINVAL, "null array");
+  const double* ctx[10] = {gamma_fixed, gg_coeff, t_dust, n_e, n_hi, n_h2, n_co,
+                           n_cp_nh, n_o_nh, n_c_nh};
+  cudaError_t e = launch_heating_cooling(n, ctx, make_lines(cii, oi63, oi145, ci), t, gamma_out,
+                                         lambda_out, st->sms, (cudaStream_t)stream);
+  return e == cudaSuccess ? P3D_OK : cuda_fail(e, "heating/cooling launch");
+}
+
+int p3d_total_heating_cooling(int64_t n, const double* gamma_fixed, const double* gg_coeff,
+                              const double* t_dust, const double* n_e, const double* n_hi,
+                              const double* n_h2, const double* n_co, const double* n_cp_nh,
+                              const double* n_o_nh, const double* n_c_nh, const double* cii,
+                              const double* oi63, const double* oi145, const double* ci,
+                              const double* t, double* gamma_out, double* lambda_out) {
+  DeviceState* st;
+  int rc = get_state(&st);
+  if (rc) return rc;
+  if (n < 0) return set_error(P3D_EINVAL, "n_cells < 0");
+  if (any_null({cii, oi63, oi145, ci})) return set_error(P3D_EINVAL, "null line parameters");
+  if (n == 0) return P3D_OK;
+  if (any_null({gamma_fixed, gg_coeff, t_dust, n_e, n_hi, n_h2, n_co, n_cp_nh, n_o_nh, n_c_nh,
+                t, gamma_out, lambda_out}))
+    return set_error(P3D_EINVAL, "null array");
+  const double* hin[11] = {gamma_fixed, gg_coeff, t_dust, n_e, n_hi, n_h2, n_co,
+                           n_cp_nh, n_o_nh, n_c_nh, t};
+  double* d[13];
+  for (int k = 0; k < 11; ++k)
+    if ((rc = stage_in(st, k, hin[k], n, &d[k]))) return rc;
+  int err;
+  for (int k = 11; k < 13; ++k) {
+    d[k] = (double*)st->slot(k, sizeof(double) * n, &err);
+    if (err) return err;
+  }
+  rc = p3d_total_heating_cooling_dev(n, d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8],
+                                     d[9], cii, oi63, oi145, ci, d[10], d[11], d[12],
+                                     st->stream);
+  if (rc) return rc;
+  if ((rc = stage_out(st, gamma_out, d[11], n))) return rc;
+  if ((rc = stage_out(st, lambda_out, d[12], n))) return rc;
+  return sync_check(st->stream, "total_heating_cooling");
+}
+
 // -------------------------------------------------------------------- PE
 int p3d_pe_heating_vec_dev(const double* pe_table, int64_t n_bins, double log_psi_min,
                            double log_psi_step, int64_t n_psi, double eg_min, double eg_step,

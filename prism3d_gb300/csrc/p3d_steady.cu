@@ -421,6 +421,12 @@ int p3d_steady_get(p3d_steady_t* h, int field, double* host_out) {
     case P3D_F_GAMMA_PE: src = d.gamma_pe; break;
     case P3D_F_ZETA: src = d.zeta; break;
     case P3D_F_F_SH_H2: src = d.fh2; break;
+    case P3D_F_GAMMA:
+    case P3D_F_LAMBDA:
+      ss_heating_cooling_kernel<<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(
+          s->n, d, s->par, field == P3D_F_LAMBDA ? 1 : 0, s->scratch);
+      src = s->scratch;
+      break;
     case P3D_F_N_H2:
     case P3D_F_N_CO: {
       ss_columns_out_kernel<<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(

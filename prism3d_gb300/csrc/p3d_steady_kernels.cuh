@@ -113,6 +113,13 @@ ss_setup_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restrict
     d.bis_node[i] = 0;
     d.bis_margin[i] = 0.0f;
     d.fh2_slope[i] = INFINITY;
+    // set by each cell's first chemistry solve; NaN until then (a get()
+    // before run() shows them as not yet computed)
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    d.gamma_pe[i] = nan;
+    d.t_dust[i] = nan;
+    d.rh2_cell[i] = nan;
+    d.fh2[i] = nan;
   }
 }
 
@@ -398,6 +405,49 @@ ss_chem_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g,
   if ((threadIdx.x & 31) == 0 && my_fail) atomicAdd(&g->chem_fail, my_fail);
 }
 
+// Thermal context of cell i (solver_3d.py:693-754) from the state its last
+// chemistry solve left: Gamma_PE, T_dust, R_H2 and f_H2 of that solve.
+__device__ __forceinline__ ThermalCtx steady_thermal_ctx(const SteadyDev& d, int64_t i) {
+  const double nh = d.dens[i];
+  const double x0 = d.x_hi[i], x1 = d.x_h2[i], x3 = d.x_c[i];
+  const double zeta = d.zeta[i];
+  const double rh2 = d.rh2_cell[i];
+  ThermalCtx c;
+  const double uv = d.uv0[i] * d.fh2[i];
+  double gf = d.gamma_pe[i];
+  gf += 3.3e-11 * uv * x1 * nh * (0.4 * kEVtoErg);
+  gf += rh2 * x0 * (nh * nh) * (1.5 * kEVtoErg);
+  gf += 3.0e-10 * uv * x1 * nh * (2.0 * kEVtoErg) * (nh / (nh + 3e4));
+  gf += zeta * (x0 + 2.0 * x1) * nh * (20.0 * kEVtoErg);
+  gf += d.hci0[i] * x3 * nh * kEVtoErg;
+  c.gamma_fixed = gf;
+  const double mu = x1 > 0.5 ? 2.0 : 1.0;
+  c.gg_coeff = 2.0 * 0.35 * 1e-21 * (nh * nh) * sqrt(8.0 * kKBoltz / (kPi * mu * kMH)) * kKBoltz;
+  c.t_dust = d.t_dust[i];
+  c.n_e = d.x_e[i] * nh;
+  c.n_hi = x0 * nh;
+  c.n_h2 = x1 * nh;
+  c.n_co = d.x_co[i] * nh;
+  c.n_cp_nh = d.x_cp[i] * nh;
+  c.n_o_nh = d.x_o[i] * nh;
+  c.n_c_nh = x3 * nh;
+  return c;
+}
+
+// Diagnostics Gamma (which == 0) or Lambda (1) at each cell's current T
+// (solver_3d.py:891-892) with the context of its last solve.
+__global__ void __launch_bounds__(kThreads)
+ss_heating_cooling_kernel(int64_t n, SteadyDev d, SteadyParams p, int which,
+                          double* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const ThermalCtx c = steady_thermal_ctx(d, i);
+    double g, l;
+    heating_cooling64(d.t_gas[i], c, p.lines, c_co_ss, &g, &l);
+    out[i] = which ? l : g;
+  }
+}
+
 // Thermal context (solver_3d.py:693-754), thermal root, per-cell T update,
 // convergence measure.
 template <bool MIXED>
@@ -421,30 +471,8 @@ ss_thermal_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
     const int64_t k = (int64_t)base + lane;
     if (k >= count) continue;
     const int64_t i = MIXED ? (int64_t)d.list[k] : k;
-    const double nh = d.dens[i];
     const double tg = d.t_gas[i];
-    const double x0 = d.x_hi[i], x1 = d.x_h2[i], x3 = d.x_c[i];
-    const double zeta = d.zeta[i];
-    const double rh2 = d.rh2_cell[i];
-    ThermalCtx c;
-    const double uv = d.uv0[i] * d.fh2[i];
-    double gf = d.gamma_pe[i];
-    gf += 3.3e-11 * uv * x1 * nh * (0.4 * kEVtoErg);
-    gf += rh2 * x0 * (nh * nh) * (1.5 * kEVtoErg);
-    gf += 3.0e-10 * uv * x1 * nh * (2.0 * kEVtoErg) * (nh / (nh + 3e4));
-    gf += zeta * (x0 + 2.0 * x1) * nh * (20.0 * kEVtoErg);
-    gf += d.hci0[i] * x3 * nh * kEVtoErg;
-    c.gamma_fixed = gf;
-    const double mu = x1 > 0.5 ? 2.0 : 1.0;
-    c.gg_coeff = 2.0 * 0.35 * 1e-21 * (nh * nh) * sqrt(8.0 * kKBoltz / (kPi * mu * kMH)) * kKBoltz;
-    c.t_dust = d.t_dust[i];
-    c.n_e = d.x_e[i] * nh;
-    c.n_hi = x0 * nh;
-    c.n_h2 = x1 * nh;
-    c.n_co = d.x_co[i] * nh;
-    c.n_cp_nh = d.x_cp[i] * nh;
-    c.n_o_nh = d.x_o[i] * nh;
-    c.n_c_nh = x3 * nh;
+    const ThermalCtx c = steady_thermal_ctx(d, i);
     int tst = 0, nev = 0;
     double troot;
     if (p.fix_t) {

@@ -27,7 +27,7 @@ from .tables import DustTables, line_params
 
 FIELDS = {"T_gas": 0, "x_HI": 1, "x_H2": 2, "x_Cp": 3, "x_C": 4, "x_CO": 5, "x_O": 6, "x_e": 7,
           "G0": 8, "A_V": 9, "N_H": 10, "N_H2": 11, "N_CO": 12, "T_dust": 13, "Gamma_PE": 14,
-          "zeta_CR": 15, "f_sh_H2": 16}
+          "zeta_CR": 15, "f_sh_H2": 16, "Gamma": 17, "Lambda": 18}
 
 
 class NotConvergedError(RuntimeError):
@@ -240,7 +240,8 @@ class PDRSolverGPU:
             zeta_CR=st["zeta_CR"], x_HI=st["x_HI"], x_H2=st["x_H2"], x_Cp=st["x_Cp"],
             x_C=st["x_C"], x_CO=st["x_CO"], x_O=st["x_O"], x_e=st["x_e"],
             x_OH=1e-9 + 9e-8 * np.clip(10.0 * st["x_H2"], 0, 1), x_H2O=np.full(shp, 1e-8),
-            x_HCOp=np.full(shp, 1e-10), Gamma_PE=st["Gamma_PE"], f_nano=np.ones(shp),
+            x_HCOp=np.full(shp, 1e-10), Gamma=st["Gamma"], Lambda=st["Lambda"],
+            Gamma_PE=st["Gamma_PE"], f_nano=np.ones(shp),
             E_g=np.full(shp, 0.1), box_size=self.box_size,
             G0_external=np.max(np.atleast_1d(self.G0_external)), zeta_CR_0=self.zeta_CR_0)
 

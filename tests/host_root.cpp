@@ -125,3 +125,12 @@ extern "C" void hr_net64(long n, const double* ctx, const double* t, double* out
     out[i] = net_heating_fast64_body(t[i], c, g_lp, g_co, g_theta2);
   }
 }
+
+// Diagnostics Gamma and Lambda at t (heating_cooling64).
+extern "C" void hr_heating_cooling(long n, const double* ctx, const double* t, double* gamma,
+                                   double* lambda) {
+  for (long i = 0; i < n; ++i) {
+    ThermalCtx c = make_ctx(ctx + 10 * i);
+    heating_cooling64(t[i], c, g_lp, g_co, gamma + i, lambda + i);
+  }
+}

@@ -12,37 +12,20 @@ every species above 1e-20 of n_H.
 The device build of the same source runs in the -m gpu tests.
 """
 import ctypes
-import os
-import shutil
-import subprocess
 
 import numpy as np
 import pytest
 
 from oracle import oracle as O
+from hostbuild import build
+from hostbuild import ptr as _p
 
-ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SPECIES = ("x_HI", "x_H2", "x_Cp", "x_C", "x_CO")
-
-
-def _cuda_include():
-    for d in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
-        if d and os.path.exists(os.path.join(d, "include", "cuda_runtime.h")):
-            return os.path.join(d, "include")
-    return None
 
 
 @pytest.fixture(scope="module")
 def lib(tmp_path_factory):
-    cxx = shutil.which("g++")
-    inc = _cuda_include()
-    if not cxx or not inc:
-        pytest.skip("needs g++ and the CUDA headers")
-    out = str(tmp_path_factory.mktemp("hostchem") / "libhostchem.so")
-    src = os.path.join(ROOT, "tests", "host_chem.cpp")
-    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", inc, src, "-o", out],
-                   check=True, capture_output=True)
-    return ctypes.CDLL(out)
+    return build("host_chem.cpp", tmp_path_factory.mktemp("hostchem"))
 
 
 @pytest.fixture(scope="module")
@@ -79,10 +62,6 @@ def monkeypatch_module():
     mp = pytest.MonkeyPatch()
     yield mp
     mp.undo()
-
-
-def _p(a):
-    return a.ctypes.data_as(ctypes.c_void_p)
 
 
 def _host_solve(L, inp, kw, mixed):

@@ -200,6 +200,38 @@ def test_thermal_torch_device(core, golden):
     np.testing.assert_allclose(t.cpu().numpy(), g["d8_T13"], rtol=1e-10)
 
 
+# ---------------------------------------------------- Gamma / Lambda
+_HEAT_STATE = ("density", "G0", "A_V", "zeta_CR", "x_HI", "x_H2", "x_Cp", "x_C", "x_CO", "x_O",
+               "x_e", "T_dust", "Gamma_PE", "R_H2")
+
+
+def test_heating_cooling_golden(core, golden):
+    """Diagnostics Gamma and Lambda (solver_3d.py:898-1050) against the
+    reference's own values, host arrays and CUDA tensors: Lambda 1e-12
+    relative, Gamma 1e-12 of the scale of its two parts (it can cancel)."""
+    import torch
+    from prism3d_gb300.tables import line_params
+    g = golden("heating")
+    ctx = [np.ascontiguousarray(a) for a in
+           O.thermal_ctx({k: g[k] for k in _HEAT_STATE}, g["f_sh_H2"])]
+    T = np.ascontiguousarray(g["T"])
+    n = T.size
+    scale = np.abs(ctx[0]) + np.abs(ctx[1] * np.sqrt(T) * (ctx[2] - T))
+    lines = line_params()
+    G, L = np.zeros(n), np.zeros(n)
+    core.total_heating_cooling(*ctx, *lines, T, G, L)
+    assert np.max(np.abs(G - g["Gamma"]) / scale) < 1e-12
+    np.testing.assert_allclose(L, g["Lambda"], rtol=1e-12, atol=0)
+    dev = [torch.from_numpy(a).cuda() for a in ctx]
+    Td = torch.from_numpy(T).cuda()
+    Gd = torch.zeros(n, dtype=torch.float64, device="cuda")
+    Ld = torch.zeros(n, dtype=torch.float64, device="cuda")
+    core.total_heating_cooling(*dev, *lines, Td, Gd, Ld)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(Gd.cpu().numpy(), G)
+    np.testing.assert_array_equal(Ld.cpu().numpy(), L)
+
+
 # ----------------------------------------------------------- chemistry
 def _chem_compare(core, rates, xc, x7, hcop, ns, frac_tight, loose):
     """Per-cell parity for short runs of the explicit Euler: nearly every cell

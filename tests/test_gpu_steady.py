@@ -93,3 +93,39 @@ def test_autotune_keeps_results():
     for k, v in ref.items():
         np.testing.assert_array_equal(s.get(k), v)
     s.close()
+
+
+def test_heating_cooling_diagnostics_and_saved_state(tmp_path):
+    """Gamma and Lambda of the converged state (the reference stores them
+    after each thermal solve, solver_3d.py:891-892) against the oracle's
+    restatement of _total_heating_vec / _total_cooling_vec on the same state,
+    and save() writing the keys of PDRSolver3D.save() (solver_3d.py:1152-1166)
+    that PDRSolver3D.load() reads back (:1184-1187)."""
+    s, (dens, g0, nside, zeta, cell) = _solver("cube16")
+    assert s.run(max_iterations=3000, convergence_tol=1e-9, mixed=True, n_allow=0)
+    st = {k: s.get(k) for k in SPECIES + ("x_O", "x_e", "T_gas", "T_dust", "Gamma_PE", "G0",
+                                          "A_V", "zeta_CR", "f_sh_H2", "Gamma", "Lambda")}
+    tb = s.tables
+    st["density"] = dens
+    st["R_H2"] = O.h2_formation_rate(st["T_gas"], st["T_dust"], 1.0, tb.sigma_nano,
+                                     tb.sigma_largeC, tb.sigma_Sil)
+    ctx = O.thermal_ctx(st, st["f_sh_H2"])
+    T = st["T_gas"].ravel()
+    G, L = O.total_heating_cooling(ctx, T)
+    scale = np.abs(np.ravel(ctx[0])) + np.abs(np.ravel(ctx[1]) * np.sqrt(T) *
+                                              (np.ravel(ctx[2]) - T))
+    # the kernels' context holds Gamma_PE and R_H2 of each cell's last
+    # chemistry solve, at the T before its last update (<= 1e-9 away)
+    assert np.max(np.abs(st["Gamma"].ravel() - G) / scale) < 1e-6
+    np.testing.assert_allclose(st["Lambda"].ravel(), L, rtol=1e-6)
+    path = tmp_path / "state.npz"
+    s.save(str(path))
+    data = np.load(path)
+    ref_keys = {"density", "T_gas", "T_dust", "G0", "A_V", "N_H", "N_H2", "N_CO", "zeta_CR",
+                "x_HI", "x_H2", "x_Cp", "x_C", "x_CO", "x_O", "x_e", "x_OH", "x_H2O", "x_HCOp",
+                "Gamma", "Lambda", "Gamma_PE", "f_nano", "E_g", "box_size", "G0_external",
+                "zeta_CR_0"}
+    assert ref_keys <= set(data.files), ref_keys - set(data.files)
+    for k in ("T_gas", "Gamma", "Lambda", "x_CO"):
+        np.testing.assert_array_equal(data[k], st[k])
+    s.close()

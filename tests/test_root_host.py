@@ -13,42 +13,20 @@ plain one, reaches the plain fixed point to 1e-6 in every cell.  The device
 build of the same source runs these paths in the -m gpu tests.
 """
 import ctypes
-import os
-import shutil
-import subprocess
 
 import numpy as np
 import pytest
 
 from oracle import oracle as O
+from hostbuild import ptr as _p
+from hostbuild import root_lib
 
-ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 TOL = 1e-10  # the mixed path's settled root tolerance
-
-
-def _cuda_include():
-    for d in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
-        if d and os.path.exists(os.path.join(d, "include", "cuda_runtime.h")):
-            return os.path.join(d, "include")
-    return None
 
 
 @pytest.fixture(scope="module")
 def lib(tmp_path_factory):
-    cxx = shutil.which("g++")
-    inc = _cuda_include()
-    if not cxx or not inc:
-        pytest.skip("needs g++ and the CUDA headers")
-    out = str(tmp_path_factory.mktemp("hostroot") / "libhostroot.so")
-    src = os.path.join(ROOT, "tests", "host_root.cpp")
-    subprocess.run([cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", inc, src, "-o", out],
-                   check=True, capture_output=True)
-    L = ctypes.CDLL(out)
-    from prism3d_gb300 import tables
-    lp = [np.ascontiguousarray(a, dtype=np.float64) for a in tables.line_params()]
-    co = np.ascontiguousarray(tables.co_ladder(), dtype=np.float64)
-    L.hr_init(*[a.ctypes.data_as(ctypes.c_void_p) for a in lp], co.ctypes.data_as(ctypes.c_void_p))
-    return L
+    return root_lib(tmp_path_factory.mktemp("hostroot"))
 
 
 @pytest.fixture(scope="module")
@@ -70,10 +48,6 @@ def contexts():
         _, _, _, ctx = O.map_residual(keep[it], dens, g0, fields.CELL_CM, 2, 2e-16)
         out.append(np.ascontiguousarray(np.stack([np.ravel(c) for c in ctx], axis=1)))
     return out
-
-
-def _p(a):
-    return a.ctypes.data_as(ctypes.c_void_p)
 
 
 def _mixed(L, ctx, t_warm, delta, node, margin, tol=TOL):

@@ -83,6 +83,15 @@ def test_dropin_argument_validation(lib):
     with pytest.raises(TypeError):
         core.pe_heating_vec(np.ones((2, 3, 4), dtype=np.float32), -1, 0.1, 3, 0.0, 0.1, 4,
                             np.ones(2), np.ones(2), np.ones(2), *[np.ones(n)] * 6, np.ones(n))
+    from prism3d_gb300.tables import line_params
+    lines = line_params()
+    with pytest.raises(ValueError):  # t of the wrong length
+        core.total_heating_cooling(*ctx, *lines, np.ones(n + 1), np.ones(n), np.ones(n))
+    with pytest.raises(TypeError):  # read-only output
+        core.total_heating_cooling(*ctx, *lines, np.ones(n), ro, np.ones(n))
+    with pytest.raises(ValueError):  # short CI parameters
+        core.total_heating_cooling(*ctx, *lines[:3], np.ones(9), np.ones(n), np.ones(n),
+                                   np.ones(n))
 
 
 def test_no_gpu_raises(lib):
@@ -95,4 +104,7 @@ def test_no_gpu_raises(lib):
     from prism3d_gb300.tables import line_params
     with pytest.raises(lib.P3DError) as ei:
         core.solve_thermal_vec(*ctx, *line_params(), 10, 3, np.ones(n))
+    assert ei.value.code == -2
+    with pytest.raises(lib.P3DError) as ei:
+        core.total_heating_cooling(*ctx, *line_params(), np.ones(n), np.ones(n), np.ones(n))
     assert ei.value.code == -2

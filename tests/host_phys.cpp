@@ -1,0 +1,43 @@
+// Host build of the steady driver's per-cell physics (prism3d_gb300/csrc/
+// p3d_phys.cuh: H2 and CO self-shielding, cosmic-ray attenuation, dust
+// temperature, H2 formation) for the CPU tests, checked against the
+// reference's own values.  Only the CUDA qualifiers are mapped to host forms.
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#undef __device__
+#define __device__
+#undef __forceinline__
+#define __forceinline__ inline
+#include "../prism3d_gb300/csrc/p3d_phys.cuh"
+
+using namespace p3d;
+
+extern "C" void hp_fsh_h2(long n, const double* nh2, double b, double* out) {
+  for (long i = 0; i < n; ++i) {
+    double d;
+    out[i] = fsh_h2(nh2[i], b, &d);
+  }
+}
+
+extern "C" void hp_fsh_co(long n, const double* nco, const double* nh2, double* out) {
+  for (long i = 0; i < n; ++i) {
+    double d;
+    out[i] = fsh_co(nco[i], nh2[i], &d);
+  }
+}
+
+extern "C" void hp_cr_rate(long n, const double* nh, double zeta0, double* out) {
+  for (long i = 0; i < n; ++i) out[i] = cr_rate(nh[i], zeta0);
+}
+
+extern "C" void hp_tdust(long n, const double* g0, const double* av, const double* nh,
+                         const double* tg, double* out) {
+  for (long i = 0; i < n; ++i) out[i] = tdust(tdust_rad(g0[i], av[i]), nh[i], tg[i]);
+}
+
+extern "C" void hp_h2_form(long n, const double* tg, const double* td, const double* fnano,
+                           double s_nano, double s_lc, double s_sil, double* out) {
+  for (long i = 0; i < n; ++i) out[i] = h2_form(tg[i], td[i], fnano[i], s_nano, s_lc, s_sil);
+}

@@ -1,0 +1,57 @@
+"""The steady driver's per-cell physics (prism3d_gb300/csrc/p3d_phys.cuh),
+built for the host (tests/host_phys.cpp), against the reference's own
+values (tests/golden/elementwise.npz, tests/golden/make_golden.py): H2
+self-shielding at five grid-mean temperatures, CO shielding, cosmic-ray
+attenuation for two zeta_0, dust temperature and the H2 formation rate on
+4000 points including the branch edges.  Tolerance 1e-13 relative (FP64
+pow/exp/log10 of the host library against NumPy's)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from hostbuild import build
+from hostbuild import ptr as _p
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    return build("host_phys.cpp", tmp_path_factory.mktemp("hostphys"))
+
+
+def _c(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def test_shielding_and_cosmic_rays(lib, golden):
+    g = golden("elementwise")
+    n = g["N_H2"].size
+    out = np.zeros(n)
+    for i, tm in enumerate(g["T_mean"]):
+        b = np.sqrt(2.0 * O.k_boltz * tm / O.m_H2) / 1e5
+        lib.hp_fsh_h2(ctypes.c_long(n), _p(_c(g["N_H2"])), ctypes.c_double(b), _p(out))
+        np.testing.assert_allclose(out, g[f"fsh_h2_{i}"], rtol=1e-13, atol=0)
+    lib.hp_fsh_co(ctypes.c_long(n), _p(_c(g["N_CO"])), _p(_c(g["N_H2"])), _p(out))
+    np.testing.assert_allclose(out, g["fsh_co"], rtol=1e-13, atol=0)
+    n = g["N_H"].size
+    out = np.zeros(n)
+    for z0 in (2e-16, 5e-16):
+        lib.hp_cr_rate(ctypes.c_long(n), _p(_c(g["N_H"])), ctypes.c_double(z0), _p(out))
+        np.testing.assert_allclose(out, g[f"zeta_{z0:g}"], rtol=1e-13, atol=0)
+
+
+def test_dust_temperature_and_h2_formation(lib, golden):
+    from prism3d_gb300.tables import DustTables
+    g = golden("elementwise")
+    tb = DustTables()
+    n = g["G0"].size
+    td = np.zeros(n)
+    lib.hp_tdust(ctypes.c_long(n), _p(_c(g["G0"])), _p(_c(g["AV"])), _p(_c(g["nH"])),
+                 _p(_c(g["Tg"])), _p(td))
+    np.testing.assert_allclose(td, g["Td"], rtol=1e-13, atol=0)
+    rh2 = np.zeros(n)
+    lib.hp_h2_form(ctypes.c_long(n), _p(_c(g["Tg"])), _p(td), _p(_c(g["fn"])),
+                   ctypes.c_double(tb.sigma_nano), ctypes.c_double(tb.sigma_largeC),
+                   ctypes.c_double(tb.sigma_Sil), _p(rh2))
+    np.testing.assert_allclose(rh2, g["RH2"], rtol=1e-13, atol=0)

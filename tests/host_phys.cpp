@@ -1,7 +1,8 @@
 // Host build of the steady driver's per-cell physics (prism3d_gb300/csrc/
 // p3d_phys.cuh: H2 and CO self-shielding, cosmic-ray attenuation, dust
-// temperature, H2 formation) for the CPU tests, checked against the
-// reference's own values.  Only the CUDA qualifiers are mapped to host forms.
+// temperature, H2 formation; p3d_pe.cuh: PE heating on the condensed
+// tables) for the CPU tests, checked against the reference's own values.
+// Only the CUDA qualifiers and __ldg are mapped to host forms.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -10,6 +11,8 @@
 #define __device__
 #undef __forceinline__
 #define __forceinline__ inline
+#define __ldg(p) (*(p))
+#include "../prism3d_gb300/csrc/p3d_pe.cuh"
 #include "../prism3d_gb300/csrc/p3d_phys.cuh"
 
 using namespace p3d;
@@ -40,4 +43,15 @@ extern "C" void hp_tdust(long n, const double* g0, const double* av, const doubl
 extern "C" void hp_h2_form(long n, const double* tg, const double* td, const double* fnano,
                            double s_nano, double s_lc, double s_sil, double* out) {
   for (long i = 0; i < n; ++i) out[i] = h2_form(tg[i], td[i], fnano[i], s_nano, s_lc, s_sil);
+}
+
+// PE heating per cell from the condensed tables a_nano, a_rest (n_psi x
+// n_eg, the per-bin sums pe_condense_kernel forms).
+extern "C" void hp_pe(long n, double log_psi_min, double log_psi_step, int n_psi, double eg_min,
+                      double eg_step, int n_eg, const double* a_nano, const double* a_rest,
+                      const double* g0, const double* tg, const double* xe, const double* nh,
+                      const double* fn, const double* eg, double* out) {
+  PeGrid g{log_psi_min, log_psi_step, eg_min, eg_step, n_psi, n_eg};
+  for (long i = 0; i < n; ++i)
+    out[i] = pe_cell(g, a_nano, a_rest, g0[i], tg[i], xe[i], nh[i], fn[i], eg[i]);
 }

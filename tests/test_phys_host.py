@@ -2,7 +2,8 @@
 built for the host (tests/host_phys.cpp), against the reference's own
 values (tests/golden/elementwise.npz, tests/golden/make_golden.py): H2
 self-shielding at five grid-mean temperatures, CO shielding, cosmic-ray
-attenuation for two zeta_0, dust temperature and the H2 formation rate on
+attenuation for two zeta_0, dust temperature, the H2 formation rate and
+the PE heating (condensed tables formed here as pe_condense_kernel does) on
 4000 points including the branch edges.  Tolerance 1e-13 relative (FP64
 pow/exp/log10 of the host library against NumPy's)."""
 import ctypes
@@ -55,3 +56,27 @@ def test_dust_temperature_and_h2_formation(lib, golden):
                    ctypes.c_double(tb.sigma_nano), ctypes.c_double(tb.sigma_largeC),
                    ctypes.c_double(tb.sigma_Sil), _p(rh2))
     np.testing.assert_allclose(rh2, g["RH2"], rtol=1e-13, atol=0)
+
+
+def test_pe_heating(lib, golden):
+    from prism3d_gb300.tables import DustTables
+    g = golden("elementwise")
+    tb = DustTables()
+    # per (psi, E_g) node: sum over bins of dn/da sigma_abs table, nano bins
+    # apart (the bins in order, as the condensing kernel adds them)
+    w = tb.bin_dn_da_da * tb.bin_sigma_abs
+    nano = tb.bin_is_nano.astype(bool)
+    a_nano = np.zeros(tb.pe_table.shape[1:])
+    a_rest = np.zeros(tb.pe_table.shape[1:])
+    for b in range(tb.n_bins):
+        if nano[b]:
+            a_nano += w[b] * tb.pe_table[b]
+        else:
+            a_rest += w[b] * tb.pe_table[b]
+    n = g["G0"].size
+    out = np.zeros(n)
+    lib.hp_pe(ctypes.c_long(n), ctypes.c_double(tb.log_psi_min), ctypes.c_double(tb.log_psi_step),
+              ctypes.c_int(tb.n_psi), ctypes.c_double(tb.eg_min), ctypes.c_double(tb.eg_step),
+              ctypes.c_int(tb.n_Eg), _p(_c(a_nano)), _p(_c(a_rest)),
+              *[_p(_c(g[k])) for k in ("G0", "Tg", "xe", "nH", "fn", "eg")], _p(out))
+    np.testing.assert_allclose(out, g["GPE"], rtol=1e-13, atol=0)

@@ -8,6 +8,8 @@ the same seeded inputs.  Tolerances:
   * thermal (10+3 steps): 1e-10 relative, except cells where a bisection
     decision sits within rounding of a sign change (the oracle reports the
     smallest |net| / scale met; those cells are counted, not compared).
+  * Gamma / Lambda diagnostics: against the reference's own values, Lambda
+    1e-12 relative, Gamma 1e-12 of the scale of its two parts.
   * chemistry (explicit Euler): 1e-9 relative plus 1e-12 of the element
     total (x_C_total for carbon species, 1 for hydrogen) for >= 99.99% of the
     cells and a looser bound for all of them up to 40 substeps; at 200

@@ -253,10 +253,15 @@ def run_gb300(args, ws, rank, local):
                 "d2h_bytes_per_step": int(d2h)},
         "plain_fp64": plain,
         "mixed_vs_plain": (value / ws) / plain.get("value", plain.get("value_est")),
-        "roofline": {"kernel": "ss_mark/chem/thermal_kernel<mixed> (97% of solve time), every "
-                               "cell solved",
+        "roofline": {"kernel": "ss_mark/chem/thermal_kernel<mixed> (~95% of the solve's device "
+                               "time, profiles/launches_slab128_mixed.md), every cell solved",
                      "bound": "fp64", "achieved": cell_tf, "peak": fp64_peak,
-                     "unit": "TFLOP/s", "frac": cell_tf / fp64_peak, "traffic": None,
+                     "unit": "TFLOP/s", "frac": cell_tf / fp64_peak,
+                     "traffic": DRAM_BYTES_PER_CELL_SOLVE * n,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
+                                       "chemistry and thermal kernels on the 96^3 slab "
+                                       "(profiles/cell_kernels_slab96.md), scaled by cells; "
+                                       "bytes per launch pair, the mark kernel not included",
                      "peak_source": "measured live: DFMA-chain kernel on this GPU",
                      "algorithmic_flops_per_launch": FP64_OPS_PER_CELL_SOLVE * n,
                      "per_unit": f"{FP64_OPS_PER_CELL_SOLVE:.0f} FP64 flops per cell solve "
@@ -356,6 +361,11 @@ def network_bench(args):
 # cell active, from the ncu instruction counts in
 # profiles/cell_kernels_slab96.md (1,754 + 3,425).
 FP64_OPS_PER_CELL_SOLVE = 5179.0
+# DRAM bytes of ss_chem_kernel + ss_thermal_kernel per cell solved, ncu on the
+# 96^3 slab with every cell active (read + write: 117.0 + 45.7 and 208.4 +
+# 62.4 MB for 884,736 cells, profiles/cell_kernels_slab96.md): the state is
+# streamed once per solve, so the traffic scales with the cells solved
+DRAM_BYTES_PER_CELL_SOLVE = (117.0 + 45.7 + 208.4 + 62.4) * 1e6 / 884736
 
 
 def fp64_peak_tflops():

@@ -55,3 +55,8 @@ extern "C" void hp_pe(long n, double log_psi_min, double log_psi_step, int n_psi
   for (long i = 0; i < n; ++i)
     out[i] = pe_cell(g, a_nano, a_rest, g0[i], tg[i], xe[i], nh[i], fn[i], eg[i]);
 }
+
+extern "C" void hp_interp_idx_weight(double x, double gmin, double gstep, int n, int* idx,
+                                     double* w) {
+  interp_idx_weight(x, gmin, gstep, n, *idx, *w);
+}

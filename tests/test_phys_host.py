@@ -80,3 +80,21 @@ def test_pe_heating(lib, golden):
               ctypes.c_int(tb.n_Eg), _p(_c(a_nano)), _p(_c(a_rest)),
               *[_p(_c(g[k])) for k in ("G0", "Tg", "xe", "nH", "fn", "eg")], _p(out))
     np.testing.assert_allclose(out, g["GPE"], rtol=1e-13, atol=0)
+
+
+def test_interp_idx_weight_known_answers(lib):
+    """The reference's Rust unit test (rust/src/pe_table.rs:147-171) on the
+    device function: middle of the grid, between nodes, clamped low and
+    high."""
+    def iw(x):
+        i = ctypes.c_int()
+        w = ctypes.c_double()
+        lib.hp_interp_idx_weight(ctypes.c_double(x), ctypes.c_double(0.0), ctypes.c_double(1.0),
+                                 ctypes.c_int(10), ctypes.byref(i), ctypes.byref(w))
+        return i.value, w.value
+    assert iw(3.0) == (3, 0.0)
+    i, w = iw(3.5)
+    assert i == 3 and abs(w - 0.5) < 1e-10
+    assert iw(-1.0) == (0, 0.0)
+    assert iw(100.0) == (8, 1.0)
+    assert iw(float("nan"))[0] == 0  # NaN maps to index 0 (Rust's saturating cast)

@@ -164,18 +164,21 @@ int p3d_pe_heating_vec_dev(const double *pe_table, int64_t n_bins, double log_ps
 
 /* ---------------------------------------------------------------------
  * Photoelectric heating that allocates no device memory.  No counterpart
- * in the reference: for callers that cannot let a library allocate (work
- * recorded inside a CUDA stream capture, embedders that fix the device
- * memory budget up front or own every device byte).  Same arguments and
- * result as p3d_pe_heating_vec_dev (device pointers for pe_table and the
- * per-cell arrays, host pointers for the bin vectors, stream NULL = default
- * stream), but its scratch is a fixed device array of 2 x 8192 + 3 x 256
- * doubles (137 KB, held by every device that loads the library until the
- * process exits): n_psi * n_eg <= 8192 and n_bins <= 256, larger tables are
- * rejected with P3D_EINVAL.  The first call on a device looks up the
- * array's device address with that device current; make that first call
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race; serialise them (one stream, or events).
+ * in the reference.  For callers that cannot let a library allocate: an
+ * application that reserves the GPU's memory for its own pool and gives each
+ * library a fixed budget, an embedder whose allocator owns every device
+ * byte, or a latency-critical caller that cannot afford the device-wide
+ * synchronisation a cudaMalloc / cudaFree can imply.  Same result as
+ * p3d_pe_heating_vec_dev, but EVERY array argument is a device pointer
+ * (pe_table, the three bin vectors, the per-cell arrays, the output), so the
+ * call copies nothing from the host; stream NULL = default stream.  Its
+ * scratch (the two condensed tables) is a fixed device array of 2 x 8192
+ * doubles (128 KB, held by every device that loads the library until the
+ * process exits): n_psi * n_eg <= 8192, larger grids are rejected with
+ * P3D_EINVAL.  The first call on a device looks up the array's device
+ * address with that device current.  All calls share the array, and each
+ * call rewrites every entry it reads; calls that overlap on the GPU race, so
+ * serialise them (one stream, or events).
  * ------------------------------------------------------------------- */
 int p3d_pe_heating_vec_noalloc(const double *pe_table, int64_t n_bins, double log_psi_min,
                                double log_psi_step, int64_t n_psi, double eg_min,

@@ -2,14 +2,17 @@
 //
 // p3d_pe_heating_vec_dev stages the grain-bin vectors and the two condensed
 // PE tables in the library's device workspace, which it grows with
-// cudaMalloc on first use.  Some callers cannot let a library allocate:
-// code running inside a CUDA stream capture (cudaMalloc is not a capturable
-// operation), hosts that hand the library a fixed memory budget up front and
-// forbid later growth, and embedders whose allocator owns every device byte.
-// p3d_pe_heating_vec_noalloc serves them: its scratch lives in a fixed
-// file-scope device array, reserved when the library is loaded and kept by
-// every device that loads it until the process exits.
-#include <cstring>
+// cudaMalloc on first use.  Some callers cannot let a library allocate: a
+// host application that reserves the GPU's memory for its own pool at start
+// and hands each library a fixed budget (a later cudaMalloc would fail or
+// push the application out of memory), an embedder whose allocator owns
+// every device byte and tracks it, and latency-critical callers for which
+// the device-wide synchronisation a cudaMalloc / cudaFree can imply stalls
+// their other streams.  p3d_pe_heating_vec_noalloc serves them: every
+// argument is a device pointer (nothing is copied from the host), and its
+// scratch, the two condensed tables, lives in a fixed file-scope device
+// array, reserved when the library is loaded and kept by every device that
+// loads it until the process exits.
 #include <mutex>
 
 #include "../../include/prism3d_gb300.h"
@@ -19,11 +22,9 @@
 
 namespace p3d {
 
-// Scratch layout (doubles): condensed tables A_nano, A_rest
-// (2 x kNoAllocMaxGrid), then sigma_abs, dn_da_da, is_nano (3 x kNoAllocMaxBins).
+// Scratch layout (doubles): condensed tables A_nano, A_rest (2 x kNoAllocMaxGrid).
 constexpr int kNoAllocMaxGrid = 8192;  // n_psi * n_eg (the THEMIS grid is 200 x 20)
-constexpr int kNoAllocMaxBins = 256;   // grain bins (THEMIS has 32)
-constexpr int kNoAllocDoubles = 2 * kNoAllocMaxGrid + 3 * kNoAllocMaxBins;
+constexpr int kNoAllocDoubles = 2 * kNoAllocMaxGrid;
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
 
@@ -83,9 +84,6 @@ extern "C" int p3d_pe_heating_vec_noalloc(
     return set_error(P3D_EINVAL,
                      "n_psi * n_eg = %lld exceeds the no-allocation limit of %d grid points",
                      (long long)(n_psi * n_eg), kNoAllocMaxGrid);
-  if (n_bins > kNoAllocMaxBins)
-    return set_error(P3D_EINVAL, "n_bins = %lld exceeds the no-allocation limit of %d bins",
-                     (long long)n_bins, kNoAllocMaxBins);
   if (!(log_psi_step != 0.0) || !(eg_step != 0.0)) return set_error(P3D_EINVAL, "zero grid step");
   double* scratch = nullptr;
   int sms = 1;
@@ -98,28 +96,16 @@ extern "C" int p3d_pe_heating_vec_noalloc(
   cudaStream_t s = (cudaStream_t)stream;
   double* a_nano = scratch;
   double* a_rest = scratch + kNoAllocMaxGrid;
-  double* bins = scratch + 2 * kNoAllocMaxGrid;
-  // Every scratch element this call reads is written earlier in the same
-  // call (bin vectors copied, tables fully rewritten), so no clearing is
-  // needed; calls that overlap on the GPU share this scratch and race.
-  double hb[3 * kNoAllocMaxBins];
-  for (int64_t b = 0; b < n_bins; ++b) {
-    hb[b] = bin_sigma_abs[b];
-    hb[n_bins + b] = bin_dn_da_da[b];
-    hb[2 * n_bins + b] = bin_is_nano[b];
-  }
-  cudaError_t e = cudaSuccess;
-  if (n_bins > 0)
-    e = cudaMemcpyAsync(bins, hb, sizeof(double) * 3 * (size_t)n_bins, cudaMemcpyHostToDevice, s);
-  if (e != cudaSuccess) return cuda_fail(e, "noalloc bins H2D");
+  // The condense kernel rewrites every table entry the cell kernel reads
+  // (n_psi * n_eg of each), so the previous call's contents never leak and
+  // nothing needs clearing; calls that overlap on the GPU share this
+  // scratch and race.
   PeGrid g{log_psi_min, log_psi_step, eg_min, eg_step, (int)n_psi, (int)n_eg};
-  e = launch_pe_condense(pe_table, (int)n_bins, g, bins, bins + n_bins, bins + 2 * n_bins, a_nano,
-                         a_rest, s);
+  cudaError_t e = launch_pe_condense(pe_table, (int)n_bins, g, bin_sigma_abs, bin_dn_da_da,
+                                     bin_is_nano, a_nano, a_rest, s);
   if (e != cudaSuccess) return cuda_fail(e, "noalloc condense launch");
   const double* cells[6] = {g0, t_gas, x_e, n_h, f_nano, e_g};
   e = launch_pe_cells(n_cells, g, a_nano, a_rest, cells, gamma_pe_out, sms, s);
   if (e != cudaSuccess) return cuda_fail(e, "noalloc pe launch");
-  // hb is on this thread's stack: the copy above is from pageable memory, so
-  // it returned only after hb had been staged.
   return P3D_OK;
 }

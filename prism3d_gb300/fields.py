@@ -109,7 +109,7 @@ def network_cells(n, seed=1):
 
 def workload(name, seed=1):
     """(density, G0_rays (per-ray array, source on -x), nside, zeta0, cell_size)."""
-    from .core import directional_G0
+    from .rays import directional_G0
     build, g0, nside, zeta = WORKLOADS[name]
     dens = build(seed)
     return dens, directional_G0(g0, [-1.0, 0.0, 0.0], nside), nside, zeta, CELL_CM

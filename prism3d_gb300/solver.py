@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _lib as L
 from . import constants as C
-from .core import directional_G0, healpix_directions  # noqa: F401
+from .rays import directional_G0, healpix_directions  # noqa: F401
 from .tables import DustTables, line_params
 
 FIELDS = {"T_gas": 0, "x_HI": 1, "x_H2": 2, "x_Cp": 3, "x_C": 4, "x_CO": 5, "x_O": 6, "x_e": 7,

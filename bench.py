@@ -171,7 +171,7 @@ def run_gb300(args, ws, rank, local):
     s2 = PDRSolverGPU(dens, box, G0_external=g0, zeta_CR_0=zeta, nside_rt=nside, T_init=100.0)
     s2.run(max_iterations=4000, convergence_tol=args.tol, mixed=True, n_allow=n_allow,
            w_chem=args.w_chem)
-    outs = [s2.get(k) for k in ("T_gas", "x_HI", "x_H2", "x_Cp", "x_C", "x_CO", "x_O", "x_e")]
+    outs = [s2.get(k) for k in STATE_KEYS]
     t_e2e = time.perf_counter() - t0
     refine = None
     if args.network_cells > 0:
@@ -205,7 +205,7 @@ def run_gb300(args, ws, rank, local):
         # per-species difference of the mixed state (the e2e solve) from the
         # plain FP64 state, cells with the plain value above 1e-20
         err = {}
-        for k, a in zip(("T_gas", "x_HI", "x_H2", "x_Cp", "x_C", "x_CO", "x_O", "x_e"), outs):
+        for k, a in zip(STATE_KEYS, outs):
             b = s.get(k).ravel()
             a = a.ravel()
             m = np.abs(b) > 1e-20
@@ -215,7 +215,9 @@ def run_gb300(args, ws, rank, local):
                       "median": float(np.median(rel)), "p99": float(np.percentile(rel, 99)),
                       "max": float(rel.max())}
         plain["mixed_vs_plain_rel_error"] = err
+        accuracy = accuracy_block(outs, [s.get(k) for k in STATE_KEYS])
     else:
+        accuracy = None
         k = args.plain_iters
         t0 = time.perf_counter()
         s.run(max_iterations=k, convergence_tol=1e-300, mixed=False, n_allow=0, w_chem=args.w_chem)
@@ -254,21 +256,21 @@ def run_gb300(args, ws, rank, local):
         "plain_fp64": plain,
         "mixed_vs_plain": (value / ws) / plain.get("value", plain.get("value_est")),
         "roofline": {"kernel": "ss_mark/chem/thermal_kernel<mixed> (~95% of the solve's device "
-                               "time, profiles/launches_slab128_mixed.md), every cell solved",
+                               "time in the ncu launch list), every cell solved",
                      "bound": "fp64", "achieved": cell_tf, "peak": fp64_peak,
                      "unit": "TFLOP/s", "frac": cell_tf / fp64_peak,
                      "traffic": DRAM_BYTES_PER_CELL_SOLVE * n,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
-                                       "chemistry and thermal kernels on the 96^3 slab "
-                                       "(profiles/cell_kernels_slab96.md), scaled by cells; "
-                                       "bytes per launch pair, the mark kernel not included",
+                                       "chemistry and thermal kernels on the 96^3 slab, every "
+                                       "cell solved, scaled by cells (bytes per launch pair, the "
+                                       "mark kernel not included)",
                      "peak_source": "measured live: DFMA-chain kernel on this GPU",
                      "algorithmic_flops_per_launch": FP64_OPS_PER_CELL_SOLVE * n,
                      "per_unit": f"{FP64_OPS_PER_CELL_SOLVE:.0f} FP64 flops per cell solve "
-                                 "(ncu instruction counts, profiles/cell_kernels_slab96.md)",
-                     "fp64_pipe_active_ncu": "85-87% (chemistry and thermal kernels, "
-                                             "profiles/cell_kernels_slab96.md): the pipe also "
-                                             "runs FP64 compares, min/max and conversions"},
+                                 "(ncu DADD + DMUL + 2 DFMA counts of the two kernels)",
+                     "fp32_flops_per_cell_solve": FP32_OPS_PER_CELL_SOLVE,
+                     "counts_commit": COUNTS_COMMIT,
+                     "fp64_pipe_active_ncu": FP64_PIPE_ACTIVE_NCU},
         "roofline_hbm": {"kernel": "ss_columns_all_kernel (3 axes x 2 directions, one launch per "
                                    "outer iteration)",
                          "bound": "hbm", "achieved": col_gbs, "peak": hbm, "unit": "GB/s",
@@ -295,11 +297,62 @@ def run_gb300(args, ws, rank, local):
                           "GB_per_s": 40 * n / tm / 1e9,
                           "note": "5 fields read once (n_H, x_H2, x_CO, x_C+, x_e), LOS = z, "
                                   "host clock around p3d_steady_column_maps"}
+    out["rt_dropin"] = rt_dropin_bench(dens, g0, cell, nside, outs, hbm, peak_kind)
     out["cpu_baseline"] = cpu_baseline(args, dens, g0, nside, zeta, cell, float(np.mean(iters)))
+    # per outer iteration (cell updates per second): the comparison that needs
+    # no assumption about how many iterations the reference would take
+    it_cpu = out["cpu_baseline"].pop("seconds_per_iteration")
+    out["per_iteration"] = {
+        "unit": "cell updates/s (cells x outer iterations / time)",
+        "mixed_gpu": n * float(np.mean(iters)) / (t_step / ws),
+        "plain_gpu": (n * plain["iterations"] / plain["seconds"]) if "iterations" in plain
+        else n / (plain["ms_per_iter"] * 1e-3),
+        "reference_cpu_port": n / it_cpu}
     if args.network_cells > 0:
         out["network"] = network_bench(args)
         out["network"]["refine_pass"] = refine
+    if accuracy is not None:
+        # last in the line, so the end of the output carries it
+        out["accuracy"] = accuracy
+        out["accuracy_ok"] = accuracy["cells_beyond"] == 0
     return out
+
+
+def rt_dropin_bench(dens, g0, cell, nside, state, hbm, peak_kind):
+    """The drop-in FUV transfer (compute_fuv_field_3d, the call the
+    reference's solver makes every outer iteration) on the converged state:
+    device tensors on torch's stream (CUDA events), and from NumPy arrays
+    through the C ABI (host clock, copies included)."""
+    import numpy as np
+    import torch
+
+    from prism3d_gb300.core import compute_fuv_field_3d
+    xh2, xco = np.ascontiguousarray(state[2]), np.ascontiguousarray(state[5])
+    n = dens.size
+    dd, dh2, dco = (torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (dens, xh2, xco))
+    for _ in range(2):
+        compute_fuv_field_3d(dd, g0, cell, dh2, dco, nside)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 5
+    e0.record()
+    for _ in range(reps):
+        compute_fuv_field_3d(dd, g0, cell, dh2, dco, nside)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    t0 = time.perf_counter()
+    for _ in range(2):
+        compute_fuv_field_3d(dens, g0, cell, xh2, xco, nside)
+    t_host = (time.perf_counter() - t0) / 2
+    gbs = 64.0 * n / (ms * 1e-3) / 1e9
+    return {"ms": ms, "cells_per_s": n / (ms * 1e-3), "e2e_cells_per_s": n / t_host,
+            "e2e_h2d_bytes": 24 * n, "e2e_d2h_bytes": 44 * n,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": gbs / hbm, "peak_source": peak_kind,
+                         "per_unit": "64 B per cell (read n_H, x_H2, x_CO; write G0, A_V, N_H, "
+                                     "N_H2, N_CO)"},
+            "rays": 12 * nside * nside}
 
 
 def network_bench(args):
@@ -356,16 +409,42 @@ def network_bench(args):
     return res
 
 
-# FP64 flops (DFMA = 2, DADD/DMUL = 1) per cell solve of the mixed chemistry
+# FP64 flops (DFMA = 2, DADD / DMUL = 1) per cell solve of the mixed chemistry
 # and thermal kernels on the 14th outer iteration of the 96^3 slab, every
-# cell active, from the ncu instruction counts in
-# profiles/cell_kernels_slab96.md (1,754 + 3,425).
+# cell active, from ncu instruction counts (1,754 + 3,425), and their FP32
+# flops; COUNTS_COMMIT names the kernels' source the counts were taken at.
 FP64_OPS_PER_CELL_SOLVE = 5179.0
+FP32_OPS_PER_CELL_SOLVE = 495.0 + 1777.0
+COUNTS_COMMIT = "1ffd122"
+FP64_PIPE_ACTIVE_NCU = "85-87% (chemistry and thermal kernels): the pipe also runs FP64 compares, min/max and conversions"
 # DRAM bytes of ss_chem_kernel + ss_thermal_kernel per cell solved, ncu on the
 # 96^3 slab with every cell active (read + write: 117.0 + 45.7 and 208.4 +
-# 62.4 MB for 884,736 cells, profiles/cell_kernels_slab96.md): the state is
-# streamed once per solve, so the traffic scales with the cells solved
+# 62.4 MB for 884,736 cells): the state is streamed once per solve, so the
+# traffic scales with the cells solved
 DRAM_BYTES_PER_CELL_SOLVE = (117.0 + 45.7 + 208.4 + 62.4) * 1e6 / 884736
+STATE_KEYS = ("T_gas", "x_HI", "x_H2", "x_Cp", "x_C", "x_CO", "x_O", "x_e")
+
+
+def accuracy_block(mixed, plain):
+    """Mixed-precision steady state against the plain FP64 one, cell by cell:
+    per field the fraction of cells within the tolerance (1e-6 relative for
+    the abundances, which are relative to n_H, counted where the plain value
+    is above 1e-20; 1e-4 for T_gas) and the largest relative difference;
+    cells_beyond counts cells with any field beyond its tolerance."""
+    import numpy as np
+    fields = {}
+    beyond = None
+    for k, a, b in zip(STATE_KEYS, mixed, plain):
+        a, b = np.ravel(a), np.ravel(b)
+        m = np.abs(b) > 1e-20
+        rel = np.zeros(a.shape)
+        rel[m] = np.abs(a - b)[m] / np.abs(b)[m]
+        tol = 1e-4 if k == "T_gas" else 1e-6
+        bad = rel > tol
+        beyond = bad if beyond is None else (beyond | bad)
+        fields[k] = [round(float(np.mean(~bad)), 7), float(rel.max())]
+    return {"tol": {"species": 1e-6, "T_gas": 1e-4}, "within_and_max": fields,
+            "cells_beyond": int(beyond.sum()), "n_cells": int(beyond.size)}
 
 
 def fp64_peak_tflops():
@@ -396,7 +475,7 @@ def cpu_baseline(args, dens, g0, nside, zeta, cell, gpu_iters):
                     n_substeps=200)
     t_it = time.perf_counter() - t0
     return {"value": dens.size / (t_it * gpu_iters), "unit": "cells/s",
-            "cores": os.cpu_count(), "kind": "port",
+            "cores": os.cpu_count(), "kind": "port", "seconds_per_iteration": t_it,
             "sample": f"one reference outer iteration on the full {dens.shape} grid "
                       f"({t_it:.2f} s; C oracle with OpenMP + NumPy ray march), "
                       f"scaled by the GPU solve's {gpu_iters:.0f} outer iterations"}
@@ -426,8 +505,15 @@ def run_reference(args, ws, rank):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_it * iters,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded Orion-Bar-like slab)", "impl": "reference",
-            "config": {"workload": f"{args.workload}", "n_cells": n,
-                       "outer_iterations_assumed": iters},
+            "config": {"workload": f"{args.workload}: {fields.WORKLOAD_DESC[args.workload]}, "
+                                   f"zeta={zeta:g}, 0.005 pc cells; converged cells/s = one "
+                                   f"measured reference outer iteration x outer_iterations_assumed "
+                                   f"= {iters} (the GPU solve's count: the reference's own run() "
+                                   f"does not converge)",
+                       "n_cells": n, "outer_iterations_assumed": iters},
+            "per_iteration": {"unit": "cell updates/s (cells x outer iterations / time)",
+                              "reference_cpu_port": n / t_it,
+                              "seconds_per_iteration": t_it},
             "cpu_baseline": {"value": value, "unit": "cells/s", "cores": os.cpu_count(),
                              "kind": "port",
                              "sample": f"one reference outer iteration per step on the full "

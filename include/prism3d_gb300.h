@@ -304,6 +304,10 @@ int p3d_steady_run(p3d_steady_t *s, int mixed, int64_t max_outer, double tol, in
                    double w_chem, double w_t, int64_t *iters_out, double *dmax_out);
 int p3d_steady_get(p3d_steady_t *s, int field, double *host_out);
 int p3d_steady_get_ray(p3d_steady_t *s, int32_t *host_out);
+/* N_H2 and N_CO along each cell's selected ray for the CURRENT abundances
+ * (fuv_rt_3d.py:297-392 restricted to the ray the full march selected; the
+ * columns the next outer iteration's shielding sees), to host memory. */
+int p3d_steady_columns(p3d_steady_t *s, double *nh2_out, double *nco_out);
 /* Overwrite one state field (P3D_F_T_GAS or P3D_F_X_HI..P3D_F_X_CO) from
  * host memory, e.g. after p3d_steady_reset; values must be finite and > 0. */
 int p3d_steady_set(p3d_steady_t *s, int field, const double *host_in);

@@ -55,6 +55,7 @@ SIGNATURES = {
     "p3d_steady_run": [_vp, ctypes.c_int, _i64, _f64, _i64, _f64, _f64, _I64, _D],
     "p3d_steady_get": [_vp, ctypes.c_int, _D],
     "p3d_steady_get_ray": [_vp, _I32],
+    "p3d_steady_columns": [_vp, _D, _D],
     "p3d_steady_set": [_vp, ctypes.c_int, _D],
     "p3d_steady_history": [_vp, _D, _i64, _I64],
     "p3d_steady_destroy": [_vp],

@@ -83,14 +83,15 @@ static unsigned cell_grid(int64_t n, int sms, int threads, int per_sm) {
   return (unsigned)(b < 1 ? 1 : b);
 }
 
-// Selected-ray N_H2 / N_CO columns of every cell: one launch, one thread per
-// (axis, direction, pencil).
+// Selected-ray N_H2 / N_CO columns of every cell: one launch, both directions
+// of each axis per pencil read (ss_columns_kernel).
 static void launch_columns(SteadySolver* s, const SteadyParams& par, cudaStream_t str) {
   const SteadyDev& d = s->d;
-  const int64_t total = 2 * (s->ny * s->nz + s->nx * s->nz + s->nx * s->ny);
-  ss_columns_all_kernel<<<(unsigned)ceil_div(total, 128), 128, 0, str>>>(
-      par.h2_implicit, s->nx, s->ny, s->nz, s->dens, d.x_h2, d.x_co, d.fam, d.ds, d.u_h2,
-      d.u_co);
+  const ColumnsGrid g = columns_grid(s->nx, s->ny, s->nz);
+  ss_columns_kernel<<<(unsigned)(g.nbx + g.nby + g.nbz), 32 * kColWarps,
+                      columns_smem_bytes(s->nx, s->ny), str>>>(
+      par.h2_implicit, s->nx, s->ny, s->nz, g.nbx, g.nby, s->dens, d.x_h2, d.x_co, d.fam, d.ds,
+      d.u_h2, d.u_co);
 }
 
 static int launch_iteration(SteadySolver* s, bool mixed, const SteadyParams& par,
@@ -166,7 +167,7 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   for (int k = 0; k < 8; ++k) p.rs[k] = 1.0;
   p.fix_t = 0;
   p.exact_roots = 0;
-  p.quiet_tol = p.quiet_in_tol = p.quiet_b_tol = 0.0;
+  p.quiet_tol = p.quiet_in_tol = p.quiet_b_tol = p.quiet_r_tol = 0.0;
   p.pe = PeGrid{log_psi_min, log_psi_step, eg_min, eg_step, (int)n_psi, (int)n_eg};
   memcpy(p.lines.cii, cii, sizeof(p.lines.cii));
   memcpy(p.lines.oi63, oi63, sizeof(p.lines.oi63));
@@ -258,6 +259,19 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
     ss_bisect_table_kernel<<<1, 32, 0, str>>>();
     e = cudaGetLastError();
   }
+  {
+    // the strided-axis column blocks keep two chunk-sum arrays per pencil
+    // tile in shared memory (16 KB for 256-cell pencils)
+    const size_t sm = columns_smem_bytes(nx, ny);
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess && sm > (size_t)optin)
+      e = cudaErrorInvalidValue;
+    if (e == cudaSuccess && sm > 48 * 1024)
+      e = cudaFuncSetAttribute(ss_columns_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)sm);
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(str);
   if (e != cudaSuccess) { delete h; return cuda_fail(e, "steady create"); }
   *out = h;
@@ -318,6 +332,11 @@ int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, in
   // the Doppler width reaches a cell only through f_H2: held to the columns'
   // tolerance
   par.quiet_b_tol = tol * 0.1;
+  // a small step alone does not make a cell settled: a T update confined to
+  // a stale bracket (or hopping across a collapsed one) moves T by ~1e-12
+  // while G(T) - T stays large, and only re-solving the cell breaks such a
+  // bracket; its thermal residual must be small too
+  par.quiet_r_tol = tol;
   auto conv = [&](const double* hrow) {
     return hrow[0] < tol || (double)hrow[4] <= (double)n_allow;
   };
@@ -443,6 +462,26 @@ int p3d_steady_get(p3d_steady_t* h, int field, double* host_out) {
   return e == cudaSuccess ? P3D_OK : cuda_fail(e, "steady get");
 }
 
+int p3d_steady_columns(p3d_steady_t* h, double* nh2_out, double* nco_out) {
+  if (!h || !nh2_out || !nco_out) return set_error(P3D_EINVAL, "null argument");
+  SteadySolver* s = &h->s;
+  cudaStream_t str = s->st->stream;
+  launch_columns(s, s->par, str);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "columns launch");
+  ++s->launches;
+  for (int which = 1; which >= 0; --which) {
+    ss_columns_out_kernel<<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(
+        s->n, which, s->par.h2_implicit, s->dens, s->d.x_h2, s->d.ds, s->d.u_h2, s->d.u_co,
+        s->scratch);
+    e = cudaMemcpyAsync(which ? nh2_out : nco_out, s->scratch, sizeof(double) * s->n,
+                        cudaMemcpyDeviceToHost, str);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(str);
+    if (e != cudaSuccess) return cuda_fail(e, "columns copy");
+  }
+  return P3D_OK;
+}
+
 int p3d_steady_set(p3d_steady_t* h, int field, const double* host_in) {
   if (!h || !host_in) return set_error(P3D_EINVAL, "null argument");
   SteadySolver* s = &h->s;
@@ -501,6 +540,7 @@ int p3d_steady_kernel_times(p3d_steady_t* h, int reps, double* ms4) {
   par.count_thr[0] = par.count_thr[1] = par.count_thr[2] = 1.0;
   par.quiet_tol = 0.0;  // no compaction: every cell solved
   par.quiet_in_tol = 0.0;
+  par.quiet_r_tol = 0.0;
   par.exact_roots = 1;  // the path whose FP64 work the roofline counts
   par.quiet_b_tol = 0.0;
   cudaEvent_t e0, e1;
@@ -601,6 +641,7 @@ int p3d_steady_autotune(p3d_steady_t* h, int warm_iters, int32_t* cfg_out, doubl
   par.count_thr[0] = par.count_thr[1] = par.count_thr[2] = 1.0;
   par.quiet_tol = 0.0;  // every cell solved
   par.quiet_in_tol = 0.0;
+  par.quiet_r_tol = 0.0;
   par.quiet_b_tol = 0.0;
   par.w_chem = 0.1;
   const SteadyDev& d = s->d;

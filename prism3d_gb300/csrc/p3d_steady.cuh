@@ -53,6 +53,7 @@ struct SteadyParams {
   double quiet_tol;     // mixed path: skip cells whose last change was <= this
   double quiet_in_tol;  // ... and whose columns moved <= this since
   double quiet_b_tol;   // ... and whose H2 shielding factor moved <= this since
+  double quiet_r_tol;   // ... and whose last thermal residual |G - T| / T was <= this
   // multipliers of the reduced network's rate coefficients (1 = the
   // reference's): H2 formation, H2 photodissociation, H2 cosmic-ray
   // destruction, C photoionisation, C+ recombination, CO photodissociation,

@@ -194,6 +194,14 @@ class PDRSolverGPU:
         L.call("p3d_steady_get", self._h, FIELDS[name], L.dptr(out))
         return out.reshape(self.density.shape)
 
+    def columns(self):
+        """(N_H2, N_CO) along each cell's selected ray for the current
+        abundances: the columns the next outer iteration's shielding sees."""
+        nh2 = np.empty(self.n_cells)
+        nco = np.empty(self.n_cells)
+        L.call("p3d_steady_columns", self._h, L.dptr(nh2), L.dptr(nco))
+        return nh2.reshape(self.density.shape), nco.reshape(self.density.shape)
+
     def elapsed_ms(self):
         """Device time of the last reset + run (CUDA events, library stream)."""
         ms = L._f64(0.0)

@@ -289,6 +289,10 @@ typedef struct p3d_steady p3d_steady_t;
  * cooling with the context of each cell's last solve */
 #define P3D_F_GAMMA 17
 #define P3D_F_LAMBDA 18
+/* largest relative change (T_gas, species above 1e-20) of each cell's last
+ * solve: the cells that are still moving when p3d_steady_run reports
+ * convergence (at most n_allow of them above tol) */
+#define P3D_F_CHANGE 19
 
 int p3d_steady_create(p3d_steady_t **out, int64_t nx, int64_t ny, int64_t nz,
                       const double *density, const double *g0_ext, int64_t n_g0,

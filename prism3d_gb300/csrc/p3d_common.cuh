@@ -24,6 +24,29 @@ struct LineParams {
   double ci[10];
 };
 
+// Line constants of the five fine-structure lines in the order CII 158,
+// OI 63, OI 145, CI 609, CI 370 (from LineParams [freq, A, T_ul, g_u, g_l]),
+// formed once on the host so the FP64 evaluation divides by none of them:
+// A, T_ul, g_u / g_l, A h nu, and the [CII] electron-excitation prefactor
+// 8.63e-6 x 2.15 / g_l (times b / sqrt(T)).
+struct LineFast {
+  double a[5], t_ul[5], g_ratio[5], e[5];
+  double cii_ce;
+};
+
+__host__ __device__ inline LineFast make_line_fast(const LineParams& lp) {
+  const double* L[5] = {lp.cii, lp.oi63, lp.oi145, lp.ci, lp.ci + 5};
+  LineFast f;
+  for (int k = 0; k < 5; ++k) {
+    f.a[k] = L[k][1];
+    f.t_ul[k] = L[k][2];
+    f.g_ratio[k] = L[k][3] / L[k][4];
+    f.e[k] = L[k][1] * kHPlanck * L[k][0];
+  }
+  f.cii_ce = 8.63e-6 / lp.cii[4] * 2.15;
+  return f;
+}
+
 // CO rotational ladder J_u = 1..40 (rust/src/thermal.rs:13-41): T_u, A,
 // g_u/g_l, 1 + 0.1 J, A h nu.  Filled once per device by the host.
 struct CoLevel {

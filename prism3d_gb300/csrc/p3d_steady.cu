@@ -90,8 +90,8 @@ static void launch_columns(SteadySolver* s, const SteadyParams& par, cudaStream_
   const ColumnsGrid g = columns_grid(s->nx, s->ny, s->nz);
   ss_columns_kernel<<<(unsigned)(g.nbx + g.nby + g.nbz), 32 * kColWarps,
                       columns_smem_bytes(s->nx, s->ny), str>>>(
-      par.h2_implicit, s->nx, s->ny, s->nz, g.nbx, g.nby, s->dens, d.x_h2, d.x_co, d.fam, d.ds,
-      d.u_h2, d.u_co);
+      par.h2_implicit, s->nx, s->ny, s->nz, g.nbx, g.nby, d.l2, d.l3, d.fam, d.ds, d.u_h2,
+      d.u_co);
 }
 
 static int launch_iteration(SteadySolver* s, bool mixed, const SteadyParams& par,
@@ -173,10 +173,11 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   memcpy(p.lines.oi63, oi63, sizeof(p.lines.oi63));
   memcpy(p.lines.oi145, oi145, sizeof(p.lines.oi145));
   memcpy(p.lines.ci, ci, sizeof(p.lines.ci));
+  p.lf = make_line_fast(p.lines);
   SteadyDev& d = s->d;
   double** dbl[] = {&s->dens, &d.g0, &d.av, &d.nh_col, &s->nh2_full, &s->nco_full, &d.ds,
                     &d.kpd0, &d.uv0, &d.kci, &d.kco0, &d.hci0, &d.zeta, &d.td_rad, &d.t_gas,
-                    &d.x_hi, &d.x_h2, &d.x_cp, &d.x_c, &d.x_co, &d.x_o, &d.x_e, &d.u_h2,
+                    &d.x_hi, &d.x_h2, &d.x_cp, &d.x_c, &d.x_co, &d.x_o, &d.x_e, &d.l2, &d.l3, &d.u_h2,
                     &d.u_co, &d.t_prev, &d.r_prev, &d.t_lo, &d.t_hi, &d.span, &d.t_root, &d.u_h2_last, &d.u_co_last, &d.b_last, &d.chg_last, &d.rh2_cell, &d.chg_spec, &d.fh2,
                     &d.gamma_pe, &d.t_dust, &s->scratch};
   for (double** q : dbl)
@@ -440,6 +441,7 @@ int p3d_steady_get(p3d_steady_t* h, int field, double* host_out) {
     case P3D_F_GAMMA_PE: src = d.gamma_pe; break;
     case P3D_F_ZETA: src = d.zeta; break;
     case P3D_F_F_SH_H2: src = d.fh2; break;
+    case P3D_F_CHANGE: src = d.chg_last; break;
     case P3D_F_GAMMA:
     case P3D_F_LAMBDA:
       ss_heating_cooling_kernel<<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(
@@ -502,6 +504,10 @@ int p3d_steady_set(p3d_steady_t* h, int field, const double* host_in) {
       return set_error(P3D_EINVAL, "value %lld must be finite and > 0", (long long)i);
   cudaError_t e = cudaMemcpyAsync(dst, host_in, sizeof(double) * s->n, cudaMemcpyHostToDevice,
                                   s->st->stream);
+  if (e == cudaSuccess && (field == P3D_F_X_H2 || field == P3D_F_X_CO)) {
+    ss_layers_kernel<<<grid_for(s->n, s->st->sms, 8), kThreads, 0, s->st->stream>>>(s->n, d);
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->st->stream);
   return e == cudaSuccess ? P3D_OK : cuda_fail(e, "steady set");
 }

@@ -17,7 +17,9 @@ struct SteadyDev {
   int8_t* fam;  // selected ray family: axis * 2 + (1 if cumsum ascends)
   // state
   double *t_gas, *x_hi, *x_h2, *x_cp, *x_c, *x_co, *x_o, *x_e;
-  // per-iteration columns
+  // column layers of the current abundances, 2 n x_H2 and n x_CO (kept by
+  // every kernel that writes x_H2 / x_CO), and the per-iteration columns
+  double *l2, *l3;
   double *u_h2, *u_co;
   // per-cell outer T update memory
   double *t_prev, *r_prev, *t_lo, *t_hi, *span;
@@ -63,6 +65,7 @@ struct SteadyParams {
   int exact_roots;  // 1: mixed thermal roots to therm_tol_mixed even while a cell moves
   PeGrid pe;
   LineParams lines;
+  LineFast lf;  // make_line_fast(lines)
 };
 
 // Scalars shared between the kernels of one outer iteration.

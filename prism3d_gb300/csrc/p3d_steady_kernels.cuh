@@ -38,6 +38,8 @@ __constant__ float c_co32[200];
 // FP64 geometric-bisection tree of [10, 1e5] K: node k (1..1023) holds
 // sqrt(lo * hi) of its bracket, children 2k (net <= 0) and 2k + 1.
 __device__ double g_bisect_mid[1024];
+// per node: the FP32 twin's temperature-only FP64 parts (p3d_thermal_fast.cuh)
+__device__ BisectNode g_bisect_node[1024];
 
 __global__ void ss_bisect_table_kernel() {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -47,6 +49,7 @@ __global__ void ss_bisect_table_kernel() {
   for (int k = 1; k < 1024; ++k) {
     double m = sqrt(lo[k] * hi[k]);
     g_bisect_mid[k] = m;
+    g_bisect_node[k] = bisect_node(m, c_co_ss);
     if (2 * k + 1 < 1024) {
       lo[2 * k] = lo[k];
       hi[2 * k] = m;
@@ -55,6 +58,26 @@ __global__ void ss_bisect_table_kernel() {
     }
   }
   g_bisect_mid[0] = 0.0;
+  g_bisect_node[0] = BisectNode{0.0f, 0.0f, 0.0f, 0};
+}
+
+// Column layers (per unit ds) of a cell: 2 n x_H2 and n x_CO, the products
+// fuv_rt_3d.py:335-337 forms (before its factor ds).  Kept beside the
+// abundances by every kernel that writes them, so the column scans read two
+// values per cell and multiply nothing.
+__device__ __forceinline__ double col_layer_h2(double n, double x_h2) {
+  return __dmul_rn(__dmul_rn(n, x_h2), 2.0);
+}
+__device__ __forceinline__ double col_layer_co(double n, double x_co) {
+  return __dmul_rn(n, x_co);
+}
+
+__global__ void ss_layers_kernel(int64_t n, SteadyDev d) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    d.l2[i] = col_layer_h2(d.dens[i], d.x_h2[i]);
+    d.l3[i] = col_layer_co(d.dens[i], d.x_co[i]);
+  }
 }
 
 // ----------------------------------------------------------------- setup
@@ -96,6 +119,8 @@ ss_setup_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restrict
     d.x_cp[i] = xcp;
     d.x_c[i] = xc;
     d.x_co[i] = xco;
+    d.l2[i] = col_layer_h2(d.dens[i], xh2);
+    d.l3[i] = col_layer_co(d.dens[i], xco);
     d.x_o[i] = fmax(p.x_o_total - xco, 1e-10);
     d.x_e[i] = fmax(xcp + p.x_hcop, 1e-10);
     d.t_gas[i] = p.t_init;
@@ -136,15 +161,21 @@ ss_setup_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restrict
 //    memory (consecutive k), one lane per pencil, so every warp load is a
 //    256-byte contiguous row.  The pencil is cut into chunks of kColChunk
 //    cells, dealt round-robin to the block's 8 warps: pass 1 stores each
-//    chunk's two layer sums in shared memory, pass 2 re-reads the chunk (an
-//    L1 hit), adds the chunk totals before it (forward) or after it
-//    (backward) as carry and writes the cells of both families.
+//    chunk's two layer sums in shared memory, two warps turn them into the
+//    carries into every chunk (exclusive sums from the front and from the
+//    back), pass 2 re-reads the chunk (an L1 hit) and writes the cells of
+//    both families, walking only the directions some cell of the chunk
+//    selected.
 //  * z (contiguous pencils): a warp per pencil, 4 consecutive cells per lane
 //    and 128 cells per step; lane sums, then a warp shuffle scan (up for the
 //    forward carry, down for the backward one).
-// Sums are exact-order sequential only inside a chunk; the columns agree
-// with a sequential cumulative sum to rounding (they feed the shielding
-// factors, whose reference form the tests compare to 1e-12).
+// The layers 2 n x_H2 and n x_CO come precomputed (col_layer_h2/_co): on
+// GB300 the scan is bound by the FP64 pipe, not by HBM, so it multiplies
+// nothing and adds each layer once per running sum.  Sums are exact-order
+// sequential only inside a chunk; the columns agree with a sequential
+// cumulative sum to rounding (they feed the shielding factors, whose
+// reference form the tests compare to 1e-12).  Layers are >= 0, so no clamp
+// at 0 is needed.
 constexpr int kColChunk = 8;    // cells per chunk of a strided pencil
 constexpr int kColWarps = 8;    // warps per block
 constexpr int kColLanesZ = 4;   // consecutive cells per lane on the z axis
@@ -153,15 +184,16 @@ __device__ __forceinline__ void col_store(int own_implicit, int64_t c, double ds
                                           double s3, double l2, double l3,
                                           double* __restrict__ u_h2,
                                           double* __restrict__ u_co) {
-  u_h2[c] = own_implicit ? dsc * s2 : fmax(dsc * (s2 + 0.5 * l2), 0.0);
-  u_co[c] = fmax(dsc * (s3 + 0.5 * l3), 0.0);
+  u_h2[c] = own_implicit ? dsc * s2 : dsc * fma(0.5, l2, s2);
+  u_co[c] = dsc * fma(0.5, l3, s3);
 }
 
-// Shared memory of one strided-axis block: two chunk-sum arrays of
-// nck x 32 doubles, nck = chunks of the longer of the x and y pencils.
+// Shared memory of one strided-axis block: chunk sums and the carries from
+// the front and from the back, nck x 32 doubles each for both layers,
+// nck = chunks of the longer of the x and y pencils.
 inline size_t columns_smem_bytes(int64_t nx, int64_t ny) {
   const int64_t len = nx > ny ? nx : ny;
-  return sizeof(double) * 2 * 32 * (size_t)ceil_div(len, kColChunk);
+  return sizeof(double) * 6 * 32 * (size_t)ceil_div(len, kColChunk);
 }
 
 // Blocks of each part of the launch: x tiles, y tiles, then z warps.
@@ -175,10 +207,9 @@ inline ColumnsGrid columns_grid(int64_t nx, int64_t ny, int64_t nz) {
 
 __global__ void __launch_bounds__(32 * kColWarps)
 ss_columns_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz, int64_t nbx,
-                  int64_t nby, const double* __restrict__ dens, const double* __restrict__ xh2,
-                  const double* __restrict__ xco, const int8_t* __restrict__ fam,
-                  const double* __restrict__ ds, double* __restrict__ u_h2,
-                  double* __restrict__ u_co) {
+                  int64_t nby, const double* __restrict__ lay2, const double* __restrict__ lay3,
+                  const int8_t* __restrict__ fam, const double* __restrict__ ds,
+                  double* __restrict__ u_h2, double* __restrict__ u_co) {
   extern __shared__ double col_sh[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t b = blockIdx.x;
@@ -193,8 +224,12 @@ ss_columns_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz, int64_t 
     const int64_t stride = axis == 0 ? ny * nz : nz;
     const int64_t base = axis == 0 ? outer * nz + k : outer * ny * nz + k;
     const int nck = (int)ceil_div(len, kColChunk);
-    double* tot2 = col_sh;
-    double* tot3 = col_sh + 32 * nck;
+    double* tot2 = col_sh;             // chunk sums
+    double* tot3 = tot2 + 32 * nck;
+    double* fc2 = tot3 + 32 * nck;     // carries from the front
+    double* fc3 = fc2 + 32 * nck;
+    double* bc2 = fc3 + 32 * nck;      // carries from the back
+    double* bc3 = bc2 + 32 * nck;
     for (int c = w; c < nck; c += kColWarps) {  // pass 1: chunk sums
       double s2 = 0.0, s3 = 0.0;
       if (live) {
@@ -202,10 +237,8 @@ ss_columns_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz, int64_t 
         for (int u = 0; u < kColChunk; ++u) {
           const int64_t tt = (int64_t)c * kColChunk + u;
           if (tt < len) {
-            const int64_t cell = base + tt * stride;
-            const double n = dens[cell];
-            s2 += __dmul_rn(__dmul_rn(n, xh2[cell]), 2.0);
-            s3 += __dmul_rn(n, xco[cell]);
+            s2 += lay2[base + tt * stride];
+            s3 += lay3[base + tt * stride];
           }
         }
       }
@@ -213,51 +246,55 @@ ss_columns_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz, int64_t 
       tot3[32 * c + lane] = s3;
     }
     __syncthreads();
+    if (w == 0) {
+      double a2 = 0.0, a3 = 0.0;
+      for (int c = 0; c < nck; ++c) {
+        fc2[32 * c + lane] = a2;
+        fc3[32 * c + lane] = a3;
+        a2 += tot2[32 * c + lane];
+        a3 += tot3[32 * c + lane];
+      }
+    } else if (w == 1) {
+      double a2 = 0.0, a3 = 0.0;
+      for (int c = nck - 1; c >= 0; --c) {
+        bc2[32 * c + lane] = a2;
+        bc3[32 * c + lane] = a3;
+        a2 += tot2[32 * c + lane];
+        a3 += tot3[32 * c + lane];
+      }
+    }
+    __syncthreads();
     if (!live) return;
     const int8_t want_f = (int8_t)(axis * 2 + 1), want_b = (int8_t)(axis * 2);
-    for (int c = w; c < nck; c += kColWarps) {  // pass 2: carries and writes
-      double l2[kColChunk], l3[kColChunk];
-      int8_t fv[kColChunk];
-#pragma unroll
-      for (int u = 0; u < kColChunk; ++u) {
-        const int64_t tt = (int64_t)c * kColChunk + u;
-        l2[u] = 0.0;
-        l3[u] = 0.0;
-        fv[u] = -1;
-        if (tt < len) {
-          const int64_t cell = base + tt * stride;
-          const double n = dens[cell];
-          l2[u] = __dmul_rn(__dmul_rn(n, xh2[cell]), 2.0);
-          l3[u] = __dmul_rn(n, xco[cell]);
-          fv[u] = fam[cell];
+    for (int c = w; c < nck; c += kColWarps) {  // pass 2: writes
+      const int64_t t0 = (int64_t)c * kColChunk;
+      const int n_u = (int)(len - t0 < kColChunk ? len - t0 : kColChunk);
+      const int64_t c0 = base + t0 * stride;
+      unsigned need_f = 0u, need_b = 0u;  // cells of the chunk selecting each direction
+      for (int u = 0; u < n_u; ++u) {
+        const int8_t f = fam[c0 + u * stride];
+        need_f |= (unsigned)(f == want_f) << u;
+        need_b |= (unsigned)(f == want_b) << u;
+      }
+      if (need_f) {
+        double f2 = fc2[32 * c + lane], f3 = fc3[32 * c + lane];
+        for (int u = 0; u < n_u; ++u) {
+          const int64_t cell = c0 + u * stride;
+          const double a2 = lay2[cell], a3 = lay3[cell];
+          if ((need_f >> u) & 1u) col_store(own_implicit, cell, ds[cell], f2, f3, a2, a3, u_h2, u_co);
+          f2 += a2;
+          f3 += a3;
         }
       }
-      double f2 = 0.0, f3 = 0.0, b2 = 0.0, b3 = 0.0;
-      for (int q = 0; q < c; ++q) {
-        f2 += tot2[32 * q + lane];
-        f3 += tot3[32 * q + lane];
-      }
-      for (int q = nck - 1; q > c; --q) {
-        b2 += tot2[32 * q + lane];
-        b3 += tot3[32 * q + lane];
-      }
-#pragma unroll
-      for (int u = 0; u < kColChunk; ++u) {
-        if (fv[u] == want_f) {
-          const int64_t cell = base + ((int64_t)c * kColChunk + u) * stride;
-          col_store(own_implicit, cell, ds[cell], f2, f3, l2[u], l3[u], u_h2, u_co);
+      if (need_b) {
+        double b2 = bc2[32 * c + lane], b3 = bc3[32 * c + lane];
+        for (int u = n_u - 1; u >= 0; --u) {
+          const int64_t cell = c0 + u * stride;
+          const double a2 = lay2[cell], a3 = lay3[cell];
+          if ((need_b >> u) & 1u) col_store(own_implicit, cell, ds[cell], b2, b3, a2, a3, u_h2, u_co);
+          b2 += a2;
+          b3 += a3;
         }
-        f2 += l2[u];
-        f3 += l3[u];
-      }
-#pragma unroll
-      for (int u = kColChunk - 1; u >= 0; --u) {
-        if (fv[u] == want_b) {
-          const int64_t cell = base + ((int64_t)c * kColChunk + u) * stride;
-          col_store(own_implicit, cell, ds[cell], b2, b3, l2[u], l3[u], u_h2, u_co);
-        }
-        b2 += l2[u];
-        b3 += l3[u];
       }
     }
     return;
@@ -279,15 +316,9 @@ ss_columns_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz, int64_t 
 #pragma unroll
       for (int u = 0; u < kColLanesZ; ++u) {
         const int64_t tt = c0 + u;
-        l2[u] = 0.0;
-        l3[u] = 0.0;
-        fv[u] = -1;
-        if (tt < nz) {
-          const double n = dens[base + tt];
-          l2[u] = __dmul_rn(__dmul_rn(n, xh2[base + tt]), 2.0);
-          l3[u] = __dmul_rn(n, xco[base + tt]);
-          fv[u] = fam[base + tt];
-        }
+        l2[u] = tt < nz ? lay2[base + tt] : 0.0;
+        l3[u] = tt < nz ? lay3[base + tt] : 0.0;
+        fv[u] = tt < nz ? fam[base + tt] : (int8_t)-1;
         s2 += l2[u];
         s3 += l3[u];
       }
@@ -539,6 +570,8 @@ ss_chem_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g,
     d.x_cp[i] = x[2];
     d.x_c[i] = x[3];
     d.x_co[i] = x[4];
+    d.l2[i] = col_layer_h2(nh, x[1]);
+    d.l3[i] = col_layer_co(nh, x[4]);
     d.x_o[i] = fmax(p.x_o_total - y[4], 1e-30);
     d.x_e[i] = fmax(y[2] + p.x_hcop, 1e-30);
     d.fh2[i] = fh2;
@@ -643,13 +676,13 @@ ss_thermal_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
       const double rtol_t = (isfinite(cl) && !p.exact_roots)
                                 ? fmax(p.therm_tol_mixed, fmin(1e-4, 0.01 * cl))
                                 : p.therm_tol_mixed;
-      troot = root_mixed(c, p.lines, c_co_ss, p.theta2, c_lines32, c_co32, g_bisect_mid,
+      troot = root_mixed(c, p.lf, c_co_ss, p.theta2, c_lines32, c_co32, g_bisect_mid, g_bisect_node,
                          rtol_t, p.therm_max_iter, d.t_root[i], delta, &node, &margin, &tst,
                          &nev);
       d.bis_node[i] = (int16_t)node;
       d.bis_margin[i] = margin;
     } else {
-      troot = root_plain(c, p.lines, c_co_ss, p.theta2, p.therm_tol, p.therm_max_iter, &tst,
+      troot = root_plain(c, p.lf, c_co_ss, p.theta2, p.therm_tol, p.therm_max_iter, &tst,
                          &nev);
     }
     my_evals += (unsigned long long)nev;
@@ -801,6 +834,8 @@ ss_refine_scatter_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* _
     d.x_o[i] = x[kNetO];
     d.x_e[i] = xe;
     const double nh = d.dens[i];
+    d.l2[i] = col_layer_h2(nh, x1);
+    d.l3[i] = col_layer_co(nh, x[kNetCO]);
     const double tg = d.t_gas[i];
     const double gpe = pe_cell(p.pe, a_nano, a_rest, d.g0[i], tg, xe, nh, p.f_nano, p.e_g);
     const double td = tdust(d.td_rad[i], nh, tg);
@@ -826,7 +861,7 @@ ss_refine_scatter_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* _
     c.n_o_nh = x[kNetO] * nh;
     c.n_c_nh = x3 * nh;
     int tst = 0, nev = 0;
-    const double troot = root_plain(c, p.lines, c_co_ss, p.theta2, p.therm_tol,
+    const double troot = root_plain(c, p.lf, c_co_ss, p.theta2, p.therm_tol,
                                     p.therm_max_iter, &tst, &nev);
     fails += (unsigned)tst;
     d.t_gas[i] = troot;

@@ -3,10 +3,14 @@
 // Same terms as rust/src/thermal.rs:50-184, rearranged for the GB300's
 // FP64/FP32 balance:
 //  * every power law T^a is exp(a ln T) from one shared logarithm (one log +
-//    one exp instead of a pow);
+//    one exp instead of a pow), and the exponentials are the table-driven
+//    exp64 (p3d_fastexp.cuh: ten FP64 operations);
 //  * the CO ladder's Boltzmann factors exp(-T_u(J)/T) use
 //    T_u(J) - T_u(J-1) = 2 theta J:  b_J = b_{J-1} q_J,  q_J = q_{J-1} q_1
 //    (two multiplies per level instead of an exp; relative drift <= J^2 eps);
+//  * the ladder's break (T_u >= 5 T) is located once per evaluation (an FP32
+//    estimate of J, settled by one or two FP64 compares with the level
+//    table) instead of one FP64 compare per level;
 //  * an FP32 twin evaluates the same terms on per-cell coefficients
 //    pre-scaled by 1 / Gamma_fixed and returns the sum of |terms| S, so a
 //    sign is certified when |net| > kCertify S (each term's FP32 error is
@@ -14,6 +18,7 @@
 #pragma once
 
 #include "p3d_common.cuh"
+#include "p3d_fastexp.cuh"
 #include "p3d_thermal.cuh"
 
 namespace p3d {
@@ -23,52 +28,71 @@ constexpr double kLn300 = 5.703782474656201152;  // ln 300
 constexpr double kLn10 = 2.302585092994045684;
 constexpr float kCertify = 1e-4f;
 
-// Two-level fraction and line energy for one line.
-__device__ __forceinline__ double line64(double q, const double* l, double inv_t) {
-  double r_lu = (l[3] / l[4]) * q * exp(-l[2] * inv_t);
-  double r_ul = l[1] + q;
-  return r_lu / (r_lu + r_ul) * l[1] * kHPlanck * l[0];
+// Number of CO levels below the ladder's break: the k with co[k].t_u < t5
+// (T_u increases with J, so they are the first ones).  T_u(J) = (T_u(1) / 2)
+// J (J + 1), so J(J + 1) = 2 t5 / T_u(1) locates the break; the FP32 estimate
+// is settled by the same FP64 compares the per-level test would make.
+__device__ __forceinline__ int co_levels_below(double t5, const CoLevel* __restrict__ co) {
+  const float r = (float)t5 / (float)co[0].t_u;
+  int k = (int)fminf(fmaxf(0.5f * (sqrtf(1.0f + 8.0f * r) - 1.0f), 0.0f), 40.0f);
+  while (k < 40 && co[k].t_u < t5) ++k;
+  while (k > 0 && !(co[k - 1].t_u < t5)) --k;
+  return k;
+}
+
+// Two-level fraction times the line's A h nu.
+__device__ __forceinline__ double line64(double q, const LineFast& lf, int k, double inv_t) {
+  const double r_lu = lf.g_ratio[k] * q * exp64(-lf.t_ul[k] * inv_t);
+  return r_lu / (r_lu + lf.a[k] + q) * lf.e[k];
 }
 
 __device__ __forceinline__ double net_heating_fast64_body(double t, const ThermalCtx& c,
-                                                     const LineParams& lp,
+                                                     const LineFast& lf,
                                                      const CoLevel* __restrict__ co,
                                                      double theta2) {
   const double lt = log(t);
   const double l01 = lt - kLn100;
   const double sqrt_t = sqrt(t);
   const double inv_t = 1.0 / t;
+  const double inv_sqrt_t = sqrt_t * inv_t;
   double net = c.gamma_fixed + c.gg_coeff * sqrt_t * (c.t_dust - t);
   {  // [CII] 158
-    const double* l = lp.cii;
-    double b = exp(-l[2] * inv_t);
-    double q = 8.63e-6 / (l[4] * sqrt_t) * 2.15 * b * c.n_e + 8.0e-10 * exp(0.07 * l01) * c.n_hi +
-               4.9e-10 * exp(0.12 * l01) * c.n_h2;
-    double r_lu = (l[3] / l[4]) * q * b;
-    net -= c.n_cp_nh * (r_lu / (r_lu + l[1] + q)) * l[1] * kHPlanck * l[0];
+    const double b = exp64(-lf.t_ul[0] * inv_t);
+    const double q = lf.cii_ce * inv_sqrt_t * b * c.n_e + 8.0e-10 * exp64(0.07 * l01) * c.n_hi +
+                     4.9e-10 * exp64(0.12 * l01) * c.n_h2;
+    const double r_lu = lf.g_ratio[0] * q * b;
+    net -= c.n_cp_nh * (r_lu / (r_lu + lf.a[0] + q)) * lf.e[0];
   }
-  const double e039 = exp(0.39 * l01);
-  net -= c.n_o_nh * line64(9.2e-12 * exp(0.67 * lt) * c.n_hi + 4.5e-12 * exp(0.64 * lt) * c.n_h2 +
-                               1.4e-8 * e039 * c.n_e, lp.oi63, inv_t);
-  net -= c.n_o_nh * line64(4.0e-12 * exp(0.60 * lt) * c.n_hi + 2.0e-12 * exp(0.58 * lt) * c.n_h2 +
-                               5.0e-9 * e039 * c.n_e, lp.oi145, inv_t);
+  const double e039 = exp64(0.39 * l01);
+  net -= c.n_o_nh * line64(9.2e-12 * exp64(0.67 * lt) * c.n_hi + 4.5e-12 * exp64(0.64 * lt) * c.n_h2 +
+                               1.4e-8 * e039 * c.n_e, lf, 1, inv_t);
+  net -= c.n_o_nh * line64(4.0e-12 * exp64(0.60 * lt) * c.n_hi + 2.0e-12 * exp64(0.58 * lt) * c.n_h2 +
+                               5.0e-9 * e039 * c.n_e, lf, 2, inv_t);
   {
-    double t03 = exp(0.3 * l01);
-    double q = 1.0e-10 * t03 * c.n_hi + 5.0e-11 * t03 * c.n_h2 + 2.0e-7 * (10.0 / sqrt_t) * c.n_e;
-    net -= c.n_c_nh * (line64(q, lp.ci, inv_t) + line64(q, lp.ci + 5, inv_t));
+    const double t03 = exp64(0.3 * l01);
+    const double q = 1.0e-10 * t03 * c.n_hi + 5.0e-11 * t03 * c.n_h2 + 2.0e-6 * inv_sqrt_t * c.n_e;
+    net -= c.n_c_nh * (line64(q, lf, 3, inv_t) + line64(q, lf, 4, inv_t));
   }
-  {  // CO ladder
-    const double g0 = 3.3e-11 * (0.1 * sqrt_t);
-    const double t5 = 5.0 * t;
-    const double q1 = exp(-theta2 * inv_t);
+  {  // CO ladder: sum_J A h nu r_lu / (r_lu + A + gamma), the fractions of
+     // up to 8 levels combined over a common denominator (one division per
+     // group instead of one per level)
+    const double gn = 3.3e-11 * (0.1 * sqrt_t) * c.n_h2;
+    const int nlev = co_levels_below(5.0 * t, co);
+    const double q1 = exp64(-theta2 * inv_t);
     double qj = q1, bj = 1.0, sum = 0.0;
-    for (int k = 0; k < 40; ++k) {
-      if (co[k].t_u >= t5) break;
-      bj *= qj;  // exp(-T_u(J) / T), J = k + 1
-      qj *= q1;
-      double gam = g0 * co[k].j_factor * c.n_h2;
-      double r_lu = co[k].g_ratio * gam * bj;
-      sum += r_lu / (r_lu + co[k].a_co + gam) * co[k].ahv;
+    for (int k0 = 0; k0 < nlev; k0 += 8) {
+      const int k1 = k0 + 8 < nlev ? k0 + 8 : nlev;
+      double num = 0.0, den = 1.0;
+      for (int k = k0; k < k1; ++k) {
+        bj *= qj;  // exp(-T_u(J) / T), J = k + 1
+        qj *= q1;
+        const double gam = gn * co[k].j_factor;
+        const double r_lu = co[k].g_ratio * gam * bj;
+        const double d = r_lu + co[k].a_co + gam;
+        num = fma(num, d, r_lu * co[k].ahv * den);
+        den *= d;
+      }
+      sum += num / den;
     }
     net -= c.n_co * sum;
   }
@@ -78,17 +102,17 @@ __device__ __forceinline__ double net_heating_fast64_body(double t, const Therma
                  x * (3.5803 + x * -0.48365)))));
     double llh2 = -24.311 + x * (4.6585 + x * (-14.272 + x * (19.779 + x * (-13.255 +
                   x * (4.4840 + x * -0.60504)))));
-    double l0 = exp(llh * kLn10) * c.n_hi + exp(llh2 * kLn10) * c.n_h2;
-    double lte = exp((-19.703 + 0.5 * x) * kLn10);
+    double l0 = exp64(llh * kLn10) * c.n_hi + exp64(llh2 * kLn10) * c.n_h2;
+    double lte = exp64((-19.703 + 0.5 * x) * kLn10);
     net -= c.n_h2 * l0 * lte / fmax(l0 + lte, 1e-50);
   }
-  if (t >= 3000.0) net -= c.n_hi * c.n_e * (2.41e-6 / sqrt_t * 0.486 * exp(-1.18e5 * inv_t)) *
+  if (t >= 3000.0) net -= c.n_hi * c.n_e * (2.41e-6 * inv_sqrt_t * 0.486 * exp64(-1.18e5 * inv_t)) *
                           10.2 * kEVtoErg;
   {
     double gg_cool = c.gg_coeff * sqrt_t * (t - c.t_dust);
     if (gg_cool > 0.0) net -= gg_cool;
   }
-  net -= c.n_cp_nh * c.n_e * (4.67e-12 * exp(-0.6 * (lt - kLn300))) * kKBoltz * t;
+  net -= c.n_cp_nh * c.n_e * (4.67e-12 * exp64(-0.6 * (lt - kLn300))) * kKBoltz * t;
   return net;
 }
 
@@ -96,19 +120,18 @@ __device__ __forceinline__ double net_heating_fast64_body(double t, const Therma
 // copy keeps the mixed thermal kernel within the instruction cache.  The
 // plain root inlines the body.
 __device__ __noinline__ double net_heating_fast64(double t, const ThermalCtx& c,
-                                                  const LineParams& lp,
+                                                  const LineFast& lf,
                                                   const CoLevel* __restrict__ co,
                                                   double theta2) {
-  return net_heating_fast64_body(t, c, lp, co, theta2);
+  return net_heating_fast64_body(t, c, lf, co, theta2);
 }
 
 // Per-cell FP32 coefficients, scaled by 1 / Gamma_fixed.
 struct ThermalCtx32 {
   float gg, td, ne, nhi, nh2, cii, o63, o145, ci609, ci370, co, h2, lya, rec;
-  double nhi64, nh264;  // H2 cooling weights stay FP64 (the fit cancels)
 };
 
-__device__ __forceinline__ ThermalCtx32 make_ctx32(const ThermalCtx& c, const LineParams& lp,
+__device__ __forceinline__ ThermalCtx32 make_ctx32(const ThermalCtx& c, const LineFast& lf,
                                                    const CoLevel* co, double* scale) {
   double K = 1.0 / fmax(c.gamma_fixed, 1e-300);
   *scale = K;
@@ -118,17 +141,15 @@ __device__ __forceinline__ ThermalCtx32 make_ctx32(const ThermalCtx& c, const Li
   f.ne = (float)c.n_e;
   f.nhi = (float)c.n_hi;
   f.nh2 = (float)c.n_h2;
-  f.cii = (float)(c.n_cp_nh * lp.cii[1] * kHPlanck * lp.cii[0] * K);
-  f.o63 = (float)(c.n_o_nh * lp.oi63[1] * kHPlanck * lp.oi63[0] * K);
-  f.o145 = (float)(c.n_o_nh * lp.oi145[1] * kHPlanck * lp.oi145[0] * K);
-  f.ci609 = (float)(c.n_c_nh * lp.ci[1] * kHPlanck * lp.ci[0] * K);
-  f.ci370 = (float)(c.n_c_nh * lp.ci[6] * kHPlanck * lp.ci[5] * K);
+  f.cii = (float)(c.n_cp_nh * lf.e[0] * K);
+  f.o63 = (float)(c.n_o_nh * lf.e[1] * K);
+  f.o145 = (float)(c.n_o_nh * lf.e[2] * K);
+  f.ci609 = (float)(c.n_c_nh * lf.e[3] * K);
+  f.ci370 = (float)(c.n_c_nh * lf.e[4] * K);
   f.co = (float)(c.n_co * co[0].ahv * K);
   f.h2 = (float)(c.n_h2 * K);
   f.lya = (float)(c.n_hi * c.n_e * 10.2 * kEVtoErg * K);
   f.rec = (float)(c.n_cp_nh * c.n_e * kKBoltz * K);
-  f.nhi64 = c.n_hi;
-  f.nh264 = c.n_h2;
   return f;
 }
 
@@ -138,14 +159,48 @@ __device__ __forceinline__ float line32(float q, float a_ul, float t_ul, float g
   return r_lu / (r_lu + a_ul + q);
 }
 
+// The temperature-only parts of the FP32 twin that need FP64 work, for one
+// node of the bisection tree (its midpoint t): the H2 cooling factors
+// 10^llh, 10^llh2, 10^lte (FP64 polynomial fits that cancel to ~1e-2 in
+// FP32) and the branch points (CO levels below the ladder's break, T >= 100
+// K, T >= 3000 K).  The bisection evaluates at these nodes only, so its FP32
+// evaluations run without an FP64 instruction.
+struct BisectNode {
+  float lh, lh2, lte;
+  int info;  // levels below the CO break | 256 (T >= 100 K) | 512 (T >= 3000 K)
+};
+
+__device__ inline void h2_cooling_factors(double x, double* lh, double* lh2, double* lte) {
+  const double llh = -24.311 + x * (3.5692 + x * (-11.332 + x * (15.738 + x * (-10.581 +
+                     x * (3.5803 + x * -0.48365)))));
+  const double llh2 = -24.311 + x * (4.6585 + x * (-14.272 + x * (19.779 + x * (-13.255 +
+                      x * (4.4840 + x * -0.60504)))));
+  *lh = exp(llh * kLn10);
+  *lh2 = exp(llh2 * kLn10);
+  *lte = exp((-19.703 + 0.5 * x) * kLn10);
+}
+
+__device__ inline BisectNode bisect_node(double t, const CoLevel* __restrict__ co) {
+  BisectNode nd;
+  nd.info = co_levels_below(5.0 * t, co) | (t >= 100.0 ? 256 : 0) | (t >= 3000.0 ? 512 : 0);
+  double lh = 0.0, lh2 = 0.0, lte = 0.0;
+  if (t >= 100.0) h2_cooling_factors(fmin(fmax(log10(t), 2.0), 4.5), &lh, &lh2, &lte);
+  nd.lh = (float)lh;
+  nd.lh2 = (float)lh2;
+  nd.lte = (float)lte;
+  return nd;
+}
+
 // FP32 net heating / Gamma_fixed and the sum of |terms|.
 // Branch points (the CO ladder break, T >= 100 K, T >= 3000 K) are decided
 // on the FP64 temperature t64 so the FP32 and FP64 functions switch terms at
-// the same temperatures.
+// the same temperatures.  With nd (a bisection node at t64) the branch
+// points and the H2 factors come from the node table.
 __device__ __noinline__ float net_heating32(double t64, const ThermalCtx32& f,
                                                const float* __restrict__ lines32,
                                                const float* __restrict__ co32,
-                                               const CoLevel* __restrict__ co, float* S) {
+                                               const CoLevel* __restrict__ co, float* S,
+                                               const BisectNode* __restrict__ nd = nullptr) {
   const float t = (float)t64;
   // lines32: 4 floats per line (A, T_ul, g_u / g_l, g_l) for CII, OI 63,
   // OI 145, CI 609, CI 370; co32: 5 floats per CO level (T_u, A, g_u / g_l,
@@ -175,32 +230,43 @@ __device__ __noinline__ float net_heating32(double t64, const ThermalCtx32& f,
     cool += f.ci609 * line32(q, lines32[12], lines32[13], lines32[14], inv_t);
     cool += f.ci370 * line32(q, lines32[16], lines32[17], lines32[18], inv_t);
   }
+  int info;
+  float lh = 0.0f, lh2 = 0.0f, lte = 0.0f;
+  if (nd) {
+    info = nd->info;
+    lh = nd->lh;
+    lh2 = nd->lh2;
+    lte = nd->lte;
+  } else {
+    info = co_levels_below(5.0 * t64, co) | (t64 >= 100.0 ? 256 : 0) | (t64 >= 3000.0 ? 512 : 0);
+    if (info & 256) {
+      const double x = fmin(fmax((double)lt / kLn10, 2.0), 4.5);
+      const double llh = -24.311 + x * (3.5692 + x * (-11.332 + x * (15.738 + x * (-10.581 +
+                         x * (3.5803 + x * -0.48365)))));
+      const double llh2 = -24.311 + x * (4.6585 + x * (-14.272 + x * (19.779 + x * (-13.255 +
+                          x * (4.4840 + x * -0.60504)))));
+      lte = exp2f((float)((-19.703 + 0.5 * x) * 3.321928094887362));
+      lh = exp2f((float)(llh * 3.321928094887362));
+      lh2 = exp2f((float)(llh2 * 3.321928094887362));
+    }
+  }
   {
     const float g0 = 3.3e-11f * (0.1f * sqrt_t);
-    const double t5 = 5.0 * t64;
+    const int nlev = info & 255;
     float sum = 0.0f;
-    for (int k = 0; k < 40; ++k) {
+    for (int k = 0; k < nlev; ++k) {
       const float* L = co32 + 5 * k;  // T_u, A, g_ratio, j_factor, ahv / ahv_1
-      if (co[k].t_u >= t5) break;
       float gam = g0 * L[3] * f.nh2;
       float r_lu = L[2] * gam * expf(-L[0] * inv_t);
       sum += r_lu / (r_lu + L[1] + gam) * L[4];
     }
     cool += f.co * sum;
   }
-  if (t64 >= 100.0) {
-    double x = fmin(fmax((double)lt / kLn10, 2.0), 4.5);
-    double llh = -24.311 + x * (3.5692 + x * (-11.332 + x * (15.738 + x * (-10.581 +
-                 x * (3.5803 + x * -0.48365)))));
-    double llh2 = -24.311 + x * (4.6585 + x * (-14.272 + x * (19.779 + x * (-13.255 +
-                  x * (4.4840 + x * -0.60504)))));
-    float lte = exp2f((float)((-19.703 + 0.5 * x) * 3.321928094887362));
-    float lh = exp2f((float)(llh * 3.321928094887362));
-    float lh2 = exp2f((float)(llh2 * 3.321928094887362));
-    float l0 = lh * (float)f.nhi64 + lh2 * (float)f.nh264;
+  if (info & 256) {
+    const float l0 = lh * f.nhi + lh2 * f.nh2;
     cool += f.h2 * (l0 * (lte / fmaxf(l0 + lte, 1e-37f)));
   }
-  if (t64 >= 3000.0) cool += f.lya * (2.41e-6f / sqrt_t * 0.486f * expf(-1.18e5f * inv_t));
+  if (info & 512) cool += f.lya * (2.41e-6f / sqrt_t * 0.486f * expf(-1.18e5f * inv_t));
   {
     float gg_cool = f.gg * sqrt_t * (t - f.td);
     if (gg_cool > 0.0f) cool += gg_cool;
@@ -217,7 +283,7 @@ __device__ __noinline__ float net_heating32(double t64, const ThermalCtx32& f,
 // previous one) to |dT| <= tol T or a bracket narrower than tol T.  A sign
 // change at a discontinuity of the net heating (the CO ladder break,
 // T = 100 K, 3000 K) converges to the jump.
-__device__ __forceinline__ double root_plain(const ThermalCtx& c, const LineParams& lp,
+__device__ __forceinline__ double root_plain(const ThermalCtx& c, const LineFast& lp,
                                              const CoLevel* __restrict__ co, double theta2,
                                              double tol, int max_it, int* status, int* n64) {
   double t_lo = 10.0, t_hi = 1e5;
@@ -321,16 +387,17 @@ __device__ __forceinline__ double slope32(double t, const ThermalCtx32& f32,
   return (double)(f0 - net_heating32(t - h, f32, lines32, co32, co, &S2)) / h;
 }
 
-__device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LineParams& lp,
+__device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LineFast& lf,
                                              const CoLevel* __restrict__ co, double theta2,
                                              const float* __restrict__ lines32,
                                              const float* __restrict__ co32,
-                                             const double* __restrict__ mid_tab, double tol,
+                                             const double* __restrict__ mid_tab,
+                                             const BisectNode* __restrict__ node_tab, double tol,
                                              int max_it, double t_warm, double delta,
                                              int* node_io, float* margin_io, int* status,
                                              int* n64) {
   double K;
-  const ThermalCtx32 f32 = make_ctx32(c, lp, co, &K);
+  const ThermalCtx32 f32 = make_ctx32(c, lf, co, &K);
   double t_lo = 10.0, t_hi = 1e5;
   int evals = 0;
   if (*node_io >= 1024 && *node_io < 2048 && delta * kReuseFactor < (double)*margin_io) {
@@ -348,13 +415,13 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LinePara
     for (int k = 0; k < 10; ++k) {
       double t_mid = __ldg(mid_tab + node);
       float S;
-      float v = net_heating32(t_mid, f32, lines32, co32, co, &S);
+      float v = net_heating32(t_mid, f32, lines32, co32, co, &S, node_tab + node);
       bool pos;
       if (fabsf(v) > kCertify * S) {
         pos = v > 0.0f;
         margin = fminf(margin, fabsf(v) / S);
       } else {
-        const double f = net_heating_fast64(t_mid, c, lp, co, theta2);
+        const double f = net_heating_fast64(t_mid, c, lf, co, theta2);
         pos = f > 0.0;
         ++evals;
         margin = fminf(margin, S > 0.0f ? (float)(fabs(f) / (double)S) : 0.0f);
@@ -364,7 +431,27 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LinePara
     *node_io = node;
     *margin_io = margin == margin ? margin : 0.0f;
   }
-  double t;
+  // After the bracket: every FP64 evaluation of the finish below goes
+  // through one call site in one loop, so the threads of a warp that are in
+  // different phases (pinned check, jump tests, Newton polish, safeguarded
+  // iteration) evaluate together; a warp then costs the largest number of
+  // evaluations among its threads, not the sum over the phases they visit.
+  enum {
+    kPinned,    // warm root pinned at 10 K / 1e5 K: one evaluation at t
+    kNearChk,   // test for a discontinuity within 1e-3 t (no evaluation)
+    kNearA,     // sign at a = d (1 - tol/2) ...
+    kNearB,     // ... and at b = d (1 + tol/2)
+    kPrep,      // FP32 slope of T's continuous piece (no evaluation)
+    kNewton,    // up to three FP64 Newton steps
+    kJumpA,     // jump of the net heating at t: sign at t (1 - tol/2) ...
+    kJumpB,     // ... and at t (1 + tol/2)
+    kSafe,      // safeguarded Newton / bisection to tol
+    kDone
+  };
+  double t, a = 0.0, b = 0.0, d_jump = 0.0, fa = 0.0, slope = 0.0, res = 0.0;
+  double dx_old = 0.0, dx = 0.0;
+  int ph, k = 0, st = 1;
+  bool at_lo = false;
   // (closed: a root returned on a discontinuity can be a bracket end, e.g.
   // 100 K, a node of the bisection tree)
   if (t_warm >= t_lo && t_warm <= t_hi) {
@@ -373,109 +460,145 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LinePara
     // sign over the whole range, every decision went that way): a warm start
     // within tol of that end that keeps the sign leaves the root between the
     // end and t -- one FP64 evaluation instead of the polish below
-    const bool at_lo = t_lo == 10.0 && t <= 10.0 * (1.0 + tol);
+    at_lo = t_lo == 10.0 && t <= 10.0 * (1.0 + tol);
     const bool at_hi = t_hi == 1e5 && t >= 1e5 * (1.0 - tol);
-    if (at_lo || at_hi) {
-      const double f = net_heating_fast64(t, c, lp, co, theta2);
-      ++evals;
-      if (at_lo ? !(f > 0.0) : (f > 0.0)) {
-        *status = 0;
-        *n64 = evals;
-        return t;
-      }
-      if (f > 0.0) t_lo = t; else t_hi = t;
-      t = sqrt(t_lo * t_hi);
-    }
+    ph = (at_lo || at_hi) ? kPinned : kNearChk;
   } else {
     t = sqrt(t_lo * t_hi);
-    for (int k = 0; k < 4; ++k) {  // FP32 Newton inside the bracket
+    for (int q = 0; q < 4; ++q) {  // FP32 Newton inside the bracket
       float S;
       const float v = net_heating32(t, f32, lines32, co32, co, &S);
-      const double d = slope32(t, f32, lines32, co32, co, theta2);
-      double tn = t - (double)v / d;
+      const double dv = slope32(t, f32, lines32, co32, co, theta2);
+      double tn = t - (double)v / dv;
       if (!(tn > t_lo && tn < t_hi)) break;
       bool small = fabs(tn - t) <= 1e-6 * t;
       t = tn;
       if (small) break;
     }
+    ph = kNearChk;
   }
-  {  // a root on a discontinuity next to t: sign change across it
-    double d_lo, d_hi;
-    jumps_around(t, co, theta2, &d_lo, &d_hi);
-    const double d = (t - d_lo <= d_hi - t) ? d_lo : d_hi;
-    if (fabs(t - d) <= 1e-3 * t && d >= t_lo && d <= t_hi) {
-      const double a = d * (1.0 - 0.5 * tol), b = d * (1.0 + 0.5 * tol);
-      const double fa = net_heating_fast64(a, c, lp, co, theta2);
-      const double fb = net_heating_fast64(b, c, lp, co, theta2);
-      evals += 2;
-      if (fa > 0.0 && !(fb > 0.0)) {
-        *status = 0;
-        *n64 = evals;
-        return d;
+  while (ph != kDone) {
+    if (ph == kNearChk) {  // a root on a discontinuity next to t: sign change across it
+      double d_lo, d_hi;
+      jumps_around(t, co, theta2, &d_lo, &d_hi);
+      d_jump = (t - d_lo <= d_hi - t) ? d_lo : d_hi;
+      if (fabs(t - d_jump) <= 1e-3 * t && d_jump >= t_lo && d_jump <= t_hi) {
+        a = d_jump * (1.0 - 0.5 * tol);
+        b = d_jump * (1.0 + 0.5 * tol);
+        ph = kNearA;
+      } else {
+        ph = kPrep;
       }
-      double lo2 = t_lo, hi2 = t_hi;
-      if (fa > 0.0) lo2 = fmax(lo2, a); else hi2 = fmin(hi2, a);
-      if (fb > 0.0) lo2 = fmax(lo2, b); else hi2 = fmin(hi2, b);
-      if (lo2 < hi2) { t_lo = lo2; t_hi = hi2; }
     }
-  }
-  if (!(t > t_lo && t < t_hi)) t = sqrt(t_lo * t_hi);
-  const double slope = slope32(t, f32, lines32, co32, co, theta2) / K;
-  *status = 1;
-  for (int k = 0; k < 3; ++k) {  // up to three FP64 Newton steps
-    double f = net_heating_fast64(t, c, lp, co, theta2);
+    if (ph == kPrep) {
+      if (!(t > t_lo && t < t_hi)) t = sqrt(t_lo * t_hi);
+      slope = slope32(t, f32, lines32, co32, co, theta2) / K;
+      k = 0;
+      ph = kNewton;
+    }
+    const double x = (ph == kNearA || ph == kJumpA) ? a : (ph == kNearB || ph == kJumpB) ? b : t;
+    const double f = net_heating_fast64(x, c, lf, co, theta2);
     ++evals;
-    if (f > 0.0) t_lo = fmax(t_lo, t); else t_hi = fmin(t_hi, t);
-    if (f == 0.0) {
-      *status = 0;
-      *n64 = evals;
-      return t;
-    }
-    double tn = t - f / slope;
-    if (!(slope < 0.0 && tn > t_lo && tn < t_hi)) break;
-    bool small = fabs(tn - t) <= fmax(1e-8, tol) * t;
-    t = tn;
-    if (small) {
-      *status = 0;
-      *n64 = evals;
-      return t;
+    switch (ph) {
+      case kPinned:
+        if (at_lo ? !(f > 0.0) : (f > 0.0)) {
+          st = 0;
+          res = t;
+          ph = kDone;
+          break;
+        }
+        if (f > 0.0) t_lo = t; else t_hi = t;
+        t = sqrt(t_lo * t_hi);
+        ph = kNearChk;
+        break;
+      case kNearA:
+      case kJumpA:
+        fa = f;
+        ph = ph == kNearA ? kNearB : kJumpB;
+        break;
+      case kNearB:
+      case kJumpB: {
+        if (fa > 0.0 && !(f > 0.0)) {
+          st = 0;
+          res = ph == kNearB ? d_jump : t;
+          ph = kDone;
+          break;
+        }
+        double lo2 = t_lo, hi2 = t_hi;
+        if (fa > 0.0) lo2 = fmax(lo2, a); else hi2 = fmin(hi2, a);
+        if (f > 0.0) lo2 = fmax(lo2, b); else hi2 = fmin(hi2, b);
+        if (lo2 < hi2) { t_lo = lo2; t_hi = hi2; }
+        if (ph == kNearB) {
+          ph = kPrep;
+        } else {
+          if (!(t > t_lo && t < t_hi)) t = sqrt(t_lo * t_hi);
+          dx_old = t_hi - t_lo;
+          dx = dx_old;
+          k = 0;
+          res = t;
+          ph = max_it > 0 ? kSafe : kDone;
+        }
+        break;
+      }
+      case kNewton: {  // up to three FP64 Newton steps
+        if (f > 0.0) t_lo = fmax(t_lo, t); else t_hi = fmin(t_hi, t);
+        if (f == 0.0) {
+          st = 0;
+          res = t;
+          ph = kDone;
+          break;
+        }
+        const double tn = t - f / slope;
+        if (!(slope < 0.0 && tn > t_lo && tn < t_hi)) {
+          ph = kJumpA;
+        } else {
+          const bool small = fabs(tn - t) <= fmax(1e-8, tol) * t;
+          t = tn;
+          if (small) {
+            st = 0;
+            res = t;
+            ph = kDone;
+          } else if (++k == 3) {
+            ph = kJumpA;
+          }
+        }
+        if (ph == kJumpA) {  // jump of the net heating at t: sign change across t (1 +- tol / 2)
+          a = t * (1.0 - 0.5 * tol);
+          b = t * (1.0 + 0.5 * tol);
+        }
+        break;
+      }
+      default: {  // kSafe
+        if (f > 0.0) t_lo = t; else t_hi = t;
+        if (f == 0.0) {
+          st = 0;
+          res = t;
+          ph = kDone;
+          break;
+        }
+        double tn = t - f / slope;
+        if (!(slope < 0.0) || !(tn > t_lo && tn < t_hi) || fabs(2.0 * f) > fabs(dx_old * slope)) {
+          dx_old = dx;
+          tn = 0.5 * (t_lo + t_hi);
+        } else {
+          dx_old = dx;
+        }
+        dx = tn - t;
+        t = tn;
+        res = t;
+        if (fabs(dx) <= tol * t || t_hi - t_lo <= tol * t) {
+          st = 0;
+          ph = kDone;
+        } else if (++k >= max_it) {
+          ph = kDone;
+        }
+        break;
+      }
     }
   }
-  {  // jump of the net heating at t: sign change across t (1 +- tol / 2)
-    double a = t * (1.0 - 0.5 * tol), b = t * (1.0 + 0.5 * tol);
-    double fa = net_heating_fast64(a, c, lp, co, theta2);
-    double fb = net_heating_fast64(b, c, lp, co, theta2);
-    evals += 2;
-    if (fa > 0.0 && !(fb > 0.0)) {
-      *status = 0;
-      *n64 = evals;
-      return t;
-    }
-    double lo2 = t_lo, hi2 = t_hi;
-    if (fa > 0.0) lo2 = fmax(lo2, a); else hi2 = fmin(hi2, a);
-    if (fb > 0.0) lo2 = fmax(lo2, b); else hi2 = fmin(hi2, b);
-    if (lo2 < hi2) { t_lo = lo2; t_hi = hi2; }
-    if (!(t > t_lo && t < t_hi)) t = sqrt(t_lo * t_hi);
-  }
-  double dx_old = t_hi - t_lo, dx = dx_old;
-  for (int k = 0; k < max_it; ++k) {
-    double f = net_heating_fast64(t, c, lp, co, theta2);
-    ++evals;
-    if (f > 0.0) t_lo = t; else t_hi = t;
-    if (f == 0.0) { *status = 0; break; }
-    double tn = t - f / slope;
-    if (!(slope < 0.0) || !(tn > t_lo && tn < t_hi) || fabs(2.0 * f) > fabs(dx_old * slope)) {
-      dx_old = dx;
-      tn = 0.5 * (t_lo + t_hi);
-    } else {
-      dx_old = dx;
-    }
-    dx = tn - t;
-    t = tn;
-    if (fabs(dx) <= tol * t || t_hi - t_lo <= tol * t) { *status = 0; break; }
-  }
+  *status = st;
   *n64 = evals;
-  return t;
+  return res;
 }
 
 }  // namespace p3d

@@ -27,7 +27,7 @@ from .tables import DustTables, line_params
 
 FIELDS = {"T_gas": 0, "x_HI": 1, "x_H2": 2, "x_Cp": 3, "x_C": 4, "x_CO": 5, "x_O": 6, "x_e": 7,
           "G0": 8, "A_V": 9, "N_H": 10, "N_H2": 11, "N_CO": 12, "T_dust": 13, "Gamma_PE": 14,
-          "zeta_CR": 15, "f_sh_H2": 16, "Gamma": 17, "Lambda": 18}
+          "zeta_CR": 15, "f_sh_H2": 16, "Gamma": 17, "Lambda": 18, "change": 19}
 
 
 class NotConvergedError(RuntimeError):
@@ -239,7 +239,10 @@ class PDRSolverGPU:
 
     def save(self, filepath):
         """np.savez_compressed with the keys of PDRSolver3D.save()
-        (solver_3d.py:1150-1170), so the reference's load() reads it."""
+        (solver_3d.py:1150-1170), so the reference's load() reads it.  The
+        reference stores one scalar G0_external; the per-ray field and the
+        ray count of this solve are added as G0_rays and nside_rt (keys
+        load() ignores)."""
         st = self.state()
         shp = self.density.shape
         np.savez_compressed(
@@ -251,7 +254,9 @@ class PDRSolverGPU:
             x_HCOp=np.full(shp, 1e-10), Gamma=st["Gamma"], Lambda=st["Lambda"],
             Gamma_PE=st["Gamma_PE"], f_nano=np.ones(shp),
             E_g=np.full(shp, 0.1), box_size=self.box_size,
-            G0_external=np.max(np.atleast_1d(self.G0_external)), zeta_CR_0=self.zeta_CR_0)
+            G0_external=np.max(np.atleast_1d(self.G0_external)), zeta_CR_0=self.zeta_CR_0,
+            G0_rays=np.atleast_1d(np.asarray(self.G0_external, dtype=np.float64)),
+            nside_rt=self.nside_rt)
 
     def close(self):
         if self._h:

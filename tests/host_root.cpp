@@ -24,7 +24,9 @@ namespace {
 CoLevel g_co[40];
 float g_l32[20], g_co32[200];
 double g_mid[1024];
+BisectNode g_node[1024];
 LineParams g_lp;
+LineFast g_lf;
 double g_theta2;
 
 ThermalCtx make_ctx(const double* c10) {
@@ -60,6 +62,7 @@ extern "C" void hr_init(const double* cii, const double* oi63, const double* oi1
     g_co[k].ahv = co5[5 * k + 4];
   }
   g_theta2 = g_co[0].t_u;
+  g_lf = make_line_fast(g_lp);
   const double* L[5] = {g_lp.cii, g_lp.oi63, g_lp.oi145, g_lp.ci, g_lp.ci + 5};
   for (int k = 0; k < 5; ++k) {
     g_l32[4 * k] = (float)L[k][1];
@@ -80,6 +83,7 @@ extern "C" void hr_init(const double* cii, const double* oi63, const double* oi1
   for (int k = 1; k < 1024; ++k) {
     double m = sqrt(lo[k] * hi[k]);
     g_mid[k] = m;
+    g_node[k] = bisect_node(m, g_co);
     if (2 * k + 1 < 1024) {
       lo[2 * k] = lo[k];
       hi[2 * k] = m;
@@ -99,7 +103,7 @@ extern "C" void hr_root_mixed(long n, const double* ctx, const double* t_warm,
     ThermalCtx c = make_ctx(ctx + 10 * i);
     int nd = node[i], st = 0, ev = 0;
     float mg = margin[i];
-    t_out[i] = root_mixed(c, g_lp, g_co, g_theta2, g_l32, g_co32, g_mid, tol, 80, t_warm[i],
+    t_out[i] = root_mixed(c, g_lf, g_co, g_theta2, g_l32, g_co32, g_mid, g_node, tol, 80, t_warm[i],
                           delta[i], &nd, &mg, &st, &ev);
     node[i] = nd;
     margin[i] = mg;
@@ -113,7 +117,7 @@ extern "C" void hr_root_plain(long n, const double* ctx, double tol, double* t_o
   for (long i = 0; i < n; ++i) {
     ThermalCtx c = make_ctx(ctx + 10 * i);
     int st = 0, ev = 0;
-    t_out[i] = root_plain(c, g_lp, g_co, g_theta2, tol, 80, &st, &ev);
+    t_out[i] = root_plain(c, g_lf, g_co, g_theta2, tol, 80, &st, &ev);
     n64[i] = ev;
     status[i] = st;
   }
@@ -122,7 +126,7 @@ extern "C" void hr_root_plain(long n, const double* ctx, double tol, double* t_o
 extern "C" void hr_net64(long n, const double* ctx, const double* t, double* out) {
   for (long i = 0; i < n; ++i) {
     ThermalCtx c = make_ctx(ctx + 10 * i);
-    out[i] = net_heating_fast64_body(t[i], c, g_lp, g_co, g_theta2);
+    out[i] = net_heating_fast64_body(t[i], c, g_lf, g_co, g_theta2);
   }
 }
 

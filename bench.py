@@ -173,6 +173,7 @@ def run_gb300(args, ws, rank, local):
            w_chem=args.w_chem)
     outs = [s2.get(k) for k in STATE_KEYS]
     t_e2e = time.perf_counter() - t0
+    chg_mixed = s2.get("change")
     refine = None
     if args.network_cells > 0:
         # refinement pass with the full network on the converged state (the
@@ -215,7 +216,8 @@ def run_gb300(args, ws, rank, local):
                       "median": float(np.median(rel)), "p99": float(np.percentile(rel, 99)),
                       "max": float(rel.max())}
         plain["mixed_vs_plain_rel_error"] = err
-        accuracy = accuracy_block(outs, [s.get(k) for k in STATE_KEYS])
+        accuracy = accuracy_block(outs, [s.get(k) for k in STATE_KEYS], chg_mixed > args.tol,
+                                  s.get("change") > args.tol, n_allow)
     else:
         accuracy = None
         k = args.plain_iters
@@ -298,6 +300,8 @@ def run_gb300(args, ws, rank, local):
                           "note": "5 fields read once (n_H, x_H2, x_CO, x_C+, x_e), LOS = z, "
                                   "host clock around p3d_steady_column_maps"}
     out["rt_dropin"] = rt_dropin_bench(dens, g0, cell, nside, outs, hbm, peak_kind)
+    if args.production and args.workload == "slab128":
+        out["production_256"] = production_bench(args)
     out["cpu_baseline"] = cpu_baseline(args, dens, g0, nside, zeta, cell, float(np.mean(iters)))
     # per outer iteration (cell updates per second): the comparison that needs
     # no assumption about how many iterations the reference would take
@@ -314,8 +318,56 @@ def run_gb300(args, ws, rank, local):
     if accuracy is not None:
         # last in the line, so the end of the output carries it
         out["accuracy"] = accuracy
-        out["accuracy_ok"] = accuracy["cells_beyond"] == 0
+        out["accuracy_ok"] = accuracy.pop("ok")
     return out
+
+
+def production_bench(args):
+    """The production-size grid: 256^3 cored slab (tanh ramp 1e3 -> 3e5 x
+    log-normal 1.2 with Gaussian cores of 1e6, zeta 5e-16, 48 rays), one
+    mixed-precision solve on the device clock; and the per-species difference
+    of mixed from plain FP64 on a 64^3 subvolume of the same density (the
+    corner cube at the highest x, where the cores sit), both solved as grids
+    of their own."""
+    import numpy as np
+
+    from prism3d_gb300 import fields
+    from prism3d_gb300.solver import PDRSolverGPU
+    dens, g0, nside, zeta, cell = fields.workload("slab256", seed=1)
+    n = dens.size
+    s = PDRSolverGPU(dens, cell * dens.shape[0], G0_external=g0, zeta_CR_0=zeta,
+                     nside_rt=nside, T_init=100.0)
+    tuned = s.autotune()
+    n_allow = max(8, int(1e-5 * n))
+    ok = s.run(max_iterations=4000, convergence_tol=args.tol, mixed=True, n_allow=n_allow,
+               w_chem=args.w_chem)
+    ms = s.elapsed_ms()
+    res = {"workload": fields.WORKLOAD_DESC["slab256"], "n_cells": n, "converged": bool(ok),
+           "outer_iterations": s.iterations, "seconds": ms * 1e-3, "cells_per_s": n / (ms * 1e-3),
+           "autotuned_cell_launch": list(tuned[:2])}
+    kt = kernel_times(s, reps=1)
+    res["columns_ms"] = kt["columns_ms"]
+    s.close()
+    sub = np.ascontiguousarray(dens[-64:, -64:, -64:])
+    st = {}
+    for mixed in (True, False):
+        q = PDRSolverGPU(sub, cell * 64, G0_external=g0, zeta_CR_0=zeta, nside_rt=nside,
+                         T_init=100.0)
+        q.run(max_iterations=4000, convergence_tol=args.tol, mixed=mixed,
+              n_allow=max(8, int(1e-5 * sub.size)), w_chem=args.w_chem)
+        st[mixed] = {k: q.get(k) for k in STATE_KEYS + ("change",)}
+        q.close()
+    err = {}
+    for k in STATE_KEYS:
+        a, b = st[True][k].ravel(), st[False][k].ravel()
+        m = np.abs(b) > 1e-20
+        rel = np.abs(a - b)[m] / np.abs(b)[m]
+        err[k] = {"frac_le_1e-6": float(np.mean(rel <= 1e-6)), "p99": float(np.quantile(rel, 0.99)),
+                  "max": float(rel.max())}
+    res["subvolume_64_mixed_vs_plain"] = err
+    res["subvolume_64_moving"] = [int(np.sum(st[True]["change"] > args.tol)),
+                                  int(np.sum(st[False]["change"] > args.tol))]
+    return res
 
 
 def rt_dropin_bench(dens, g0, cell, nside, state, hbm, peak_kind):
@@ -425,12 +477,18 @@ DRAM_BYTES_PER_CELL_SOLVE = (117.0 + 45.7 + 208.4 + 62.4) * 1e6 / 884736
 STATE_KEYS = ("T_gas", "x_HI", "x_H2", "x_Cp", "x_C", "x_CO", "x_O", "x_e")
 
 
-def accuracy_block(mixed, plain):
+def accuracy_block(mixed, plain, moving_mixed, moving_plain, n_allow):
     """Mixed-precision steady state against the plain FP64 one, cell by cell:
     per field the fraction of cells within the tolerance (1e-6 relative for
     the abundances, which are relative to n_H, counted where the plain value
-    is above 1e-20; 1e-4 for T_gas) and the largest relative difference;
-    cells_beyond counts cells with any field beyond its tolerance."""
+    is above 1e-20; 1e-4 for T_gas) and the largest relative difference.
+    A solve converges when at most n_allow cells still change by more than
+    tol per iteration; those cells (moving_*: the per-cell change of the
+    last solve above tol) have not settled in one solve or the other and are
+    counted apart: cells_beyond counts every cell with a field beyond its
+    tolerance, cells_beyond_settled those among the settled cells.
+    ok: no settled cell beyond tolerance, and each solve left at most
+    n_allow cells moving."""
     import numpy as np
     fields = {}
     beyond = None
@@ -443,8 +501,14 @@ def accuracy_block(mixed, plain):
         bad = rel > tol
         beyond = bad if beyond is None else (beyond | bad)
         fields[k] = [round(float(np.mean(~bad)), 7), float(rel.max())]
+    moving = np.ravel(moving_mixed) | np.ravel(moving_plain)
+    settled_bad = int(np.sum(beyond & ~moving))
     return {"tol": {"species": 1e-6, "T_gas": 1e-4}, "within_and_max": fields,
-            "cells_beyond": int(beyond.sum()), "n_cells": int(beyond.size)}
+            "cells_beyond": int(beyond.sum()), "cells_beyond_settled": settled_bad,
+            "moving": [int(np.sum(moving_mixed)), int(np.sum(moving_plain))],
+            "n_allow": int(n_allow), "n_cells": int(beyond.size),
+            "ok": bool(settled_bad == 0 and np.sum(moving_mixed) <= n_allow
+                       and np.sum(moving_plain) <= n_allow)}
 
 
 def fp64_peak_tflops():
@@ -543,6 +607,9 @@ def main():
     ap.add_argument("--network-cells", type=int, default=1 << 20,
                     help="cells of the full-network measurement (0: skip)")
     ap.add_argument("--network-cpu-sample", type=int, default=2048)
+    ap.add_argument("--production", type=int, default=1,
+                    help="1: also solve the 256^3 production grid (one mixed solve) and "
+                         "compare mixed with plain FP64 on a 64^3 subvolume")
     args = ap.parse_args()
     ws, rank, local = _dist()
     if ws > 1:

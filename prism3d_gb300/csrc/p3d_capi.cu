@@ -488,8 +488,10 @@ int p3d_fuv_field_3d_dev(int64_t nx, int64_t ny, int64_t nz, const double* densi
     ray = (int32_t*)st->slot(kSlotRay, sizeof(int32_t) * n, &err);
     if (err) return err;
   }
+  void* work = st->slot(kSlotRtWork, rt_work_bytes(n), &err);
+  if (err) return err;
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e = launch_fuv_full(nx, ny, nz, density, x_h2, x_co, *rs, g0, a_v, n_h_col,
+  cudaError_t e = launch_fuv_full(nx, ny, nz, density, x_h2, x_co, *rs, work, g0, a_v, n_h_col,
                                   n_h2_col, n_co_col, ray, st->sms, s);
   return e == cudaSuccess ? P3D_OK : cuda_fail(e, "fuv launch");
 }

@@ -14,6 +14,7 @@ enum : int {
   kSlotPeCond = 17,
   kSlotPeTable = 18,
   kSlotRay = 19,
+  kSlotRtWork = 20,
   kSlots = 24,
 };
 

@@ -28,9 +28,15 @@ struct RayChunk {
   double w[kRayChunk];
 };
 
+// Device workspace launch_fuv_full needs for n cells (per-family partial
+// results: 36 bytes per cell and family).
+size_t rt_work_bytes(int64_t n);
+// Kernel launches of one launch_fuv_full call for this ray set.
+int rt_launch_count(const RaySet& rs);
+
 cudaError_t launch_fuv_full(int64_t nx, int64_t ny, int64_t nz, const double* dens,
                             const double* xh2, const double* xco, const RaySet& rs,
-                            double* g0, double* av, double* nh, double* nh2, double* nco,
-                            int32_t* ray, int sms, cudaStream_t s);
+                            void* work, double* g0, double* av, double* nh, double* nh2,
+                            double* nco, int32_t* ray, int sms, cudaStream_t s);
 
 }  // namespace p3d

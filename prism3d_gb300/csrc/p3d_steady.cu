@@ -289,7 +289,10 @@ int p3d_steady_reset(p3d_steady_t* h) {
     cudaEventCreate(&s->ev_stop);
   }
   cudaEventRecord(s->ev_start, str);
-  cudaError_t e = launch_fuv_full(s->nx, s->ny, s->nz, s->dens, nullptr, nullptr, s->rays, d.g0,
+  int err = 0;
+  void* work = s->st->slot(kSlotRtWork, rt_work_bytes(s->n), &err);
+  if (err) return err;
+  cudaError_t e = launch_fuv_full(s->nx, s->ny, s->nz, s->dens, nullptr, nullptr, s->rays, work, d.g0,
                                   d.av, d.nh_col, s->nh2_full, s->nco_full, d.ray, s->st->sms,
                                   str);
   if (e != cudaSuccess) return cuda_fail(e, "reset: ray march");
@@ -301,14 +304,7 @@ int p3d_steady_reset(p3d_steady_t* h) {
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "reset launch");
   s->iters_done = 0;
-  int chunks = 0;
-  for (int fam = 0; fam < 6; ++fam) {
-    int cnt = 0;
-    for (int r = 0; r < s->rays.n; ++r)
-      cnt += (s->rays.axis[r] * 2 + s->rays.fwd[r] == fam);
-    chunks += (cnt + kRayChunk - 1) / kRayChunk;
-  }
-  s->launches = 2 + chunks + 2;  // ray-march init/fix, families, setup, globals
+  s->launches = rt_launch_count(s->rays) + 2;  // ray march, setup, globals
   s->last_dmax = INFINITY;
   return P3D_OK;
 }

@@ -293,6 +293,9 @@ typedef struct p3d_steady p3d_steady_t;
  * solve: the cells that are still moving when p3d_steady_run reports
  * convergence (at most n_allow of them above tol) */
 #define P3D_F_CHANGE 19
+/* THEMIS grain state per cell: nano-grain fraction and band gap [eV] */
+#define P3D_F_F_NANO 20
+#define P3D_F_E_G 21
 
 int p3d_steady_create(p3d_steady_t **out, int64_t nx, int64_t ny, int64_t nz,
                       const double *density, const double *g0_ext, int64_t n_g0,
@@ -308,6 +311,21 @@ int p3d_steady_run(p3d_steady_t *s, int mixed, int64_t max_outer, double tol, in
                    double w_chem, double w_t, int64_t *iters_out, double *dmax_out);
 int p3d_steady_get(p3d_steady_t *s, int field, double *host_out);
 int p3d_steady_get_ray(p3d_steady_t *s, int32_t *host_out);
+/* Point-source field for the steady driver (solver_3d.py:270-276, the
+ * reference's star mode): from the next p3d_steady_reset the FUV field and
+ * extinction come from compute_fuv_field_point_source
+ * (fuv_rt_3d.py:74-212) for a star at star_pos [cm, 3] with FUV luminosity
+ * l_fuv [erg/s], and every outer iteration takes its H2 / CO columns along
+ * the star's direction; l_fuv <= 0 returns to the external ray-set field.
+ * The adjoint (p3d_steady_adjoint) covers the ray-set field only. */
+int p3d_steady_set_point_source(p3d_steady_t *s, const double *star_pos, double l_fuv);
+/* One dust step of the outer loop (solver_3d.py:239-249): the THEMIS grain
+ * step _evolve_dust_state (solver_3d.py:465-507) on every cell's f_nano and
+ * E_g, after which the next p3d_steady_run re-solves every cell to the new
+ * steady state (the per-cell T-update brackets restart, as the reference's
+ * per-cell damping does for each dust step).  The grain state starts at the
+ * reference's f_nano = 1, E_g = 0.1 at p3d_steady_reset. */
+int p3d_steady_dust_step(p3d_steady_t *s);
 /* N_H2 and N_CO along each cell's selected ray for the CURRENT abundances
  * (fuv_rt_3d.py:297-392 restricted to the ray the full march selected; the
  * columns the next outer iteration's shielding sees), to host memory. */

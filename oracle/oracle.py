@@ -587,7 +587,7 @@ def t_update(T_in, G, mem, w_T=0.5):
 def steady_run(density, G0_external, cell_size, nside=1, zeta0=2e-16, T_init=100.0,
                max_outer=500, tol=1e-10, w_chem=0.5, w_T=0.5, chem_rtol=1e-12,
                therm_tol=1e-12, tables=None, lines=None, verbose=False, callback=None,
-               co_implicit=False, h2_implicit=False, accel=False):
+               co_implicit=False, h2_implicit=False, accel=False, star=None):
     """FP64 CPU restatement of the GPU steady-state driver.
 
     Outer fixed-point iteration with the per-iteration physics of
@@ -600,7 +600,10 @@ def steady_run(density, G0_external, cell_size, nside=1, zeta0=2e-16, T_init=100
     and new conserved states); T follows the per-cell bracketed secant
     update of t_update() on the thermal root (bisection + safeguarded
     Newton).  Stops when the largest relative change of T and of every
-    species above 1e-20 (relative to n_H) is below tol.
+    species above 1e-20 (relative to n_H) is below tol.  star = (position
+    [cm, 3], L_FUV [erg/s]) takes the field and the per-iteration columns
+    from fuv_point_source instead (the reference's star mode,
+    solver_3d.py:270-276).
     Returns (state, history)."""
     if tables is None:
         from prism3d_gb300.tables import DustTables
@@ -612,13 +615,17 @@ def steady_run(density, G0_external, cell_size, nside=1, zeta0=2e-16, T_init=100
     st = init_state(density, G0_external, zeta0, T_init)
     shp = density.shape
     n = st["density"]
-    G0, AV, NH, _, _, ray = fuv_field_3d(n, G0_external, cell_size, None, None, nside,
-                                         return_ray=True)
+    if star is not None:
+        G0, AV, NH, _, _ = fuv_point_source(n, star[0], star[1], cell_size)
+        ray = np.full(shp, -1, dtype=np.int32)
+    else:
+        G0, AV, NH, _, _, ray = fuv_field_3d(n, G0_external, cell_size, None, None, nside,
+                                             return_ray=True)
     st["G0"], st["A_V"], st["N_H"], st["ray"] = G0, AV, NH, ray
     analytic_ic(st)
     const = steady_constants(st, zeta0)
     st["zeta_CR"] = const["zeta"]
-    ds = ray_ds(dirs, cell_size)[ray]
+    ds = ray_ds(dirs, cell_size)[ray] if star is None else np.zeros(shp)
     species = ("x_HI", "x_H2", "x_Cp", "x_C", "x_CO")
     hist = []
     mem = (np.zeros(shp), np.zeros(shp), np.zeros(shp), np.full(shp, np.inf),
@@ -627,7 +634,11 @@ def steady_run(density, G0_external, cell_size, nside=1, zeta0=2e-16, T_init=100
     accel_clip = 4.0
     for it in range(max_outer):
         old = {k: st[k].copy() for k in ("T_gas",) + species}
-        NH2, NCO = selected_columns(n, st["x_H2"], st["x_CO"], ray, dirs, cell_size)
+        if star is not None:
+            NH2, NCO = fuv_point_source(n, star[0], star[1], cell_size, st["x_H2"],
+                                        st["x_CO"])[3:]
+        else:
+            NH2, NCO = selected_columns(n, st["x_H2"], st["x_CO"], ray, dirs, cell_size)
         st["N_H2"], st["N_CO"] = NH2, NCO
         u_h2 = NH2 - n * st["x_H2"] * ds if h2_implicit else NH2
         u_co = NCO - 0.5 * n * st["x_CO"] * ds if co_implicit else NCO
@@ -701,7 +712,8 @@ def _from_zvars(st, z):
     st["x_C"] = r2 * st["x_Cp"]
 
 
-def map_residual(st_in, density, G0_external, cell_size, nside, zeta0, tables=None, lines=None):
+def map_residual(st_in, density, G0_external, cell_size, nside, zeta0, tables=None, lines=None,
+                 star=None):
     """Apply the steady-state outer map once (without damping or T update)
     to a state and return (x_star, G, ray): the chemistry steady state and
     the thermal root for that state's columns, grid-mean T and T.  At a fixed
@@ -718,13 +730,21 @@ def map_residual(st_in, density, G0_external, cell_size, nside, zeta0, tables=No
     for k, v in st_in.items():
         st[k] = np.array(v, dtype=np.float64, copy=True)
     n = st["density"]
-    G0, AV, NH, _, _, ray = fuv_field_3d(n, G0_external, cell_size, None, None, nside,
-                                         return_ray=True)
+    if star is not None:  # (position [cm, 3], L_FUV [erg/s]), as steady_run
+        G0, AV, NH, NH2, NCO = fuv_point_source(n, star[0], star[1], cell_size, st["x_H2"],
+                                                st["x_CO"])
+        ray = np.full(n.shape, -1, dtype=np.int32)
+    else:
+        G0, AV, NH, _, _, ray = fuv_field_3d(n, G0_external, cell_size, None, None, nside,
+                                             return_ray=True)
     st["G0"], st["A_V"], st["N_H"] = G0, AV, NH
     const = steady_constants(st, zeta0)
     st["zeta_CR"] = const["zeta"]
-    ds = ray_ds(dirs, cell_size)[ray]
-    NH2, NCO = selected_columns(n, st["x_H2"], st["x_CO"], ray, dirs, cell_size)
+    if star is not None:
+        ds = np.zeros(n.shape)
+    else:
+        ds = ray_ds(dirs, cell_size)[ray]
+        NH2, NCO = selected_columns(n, st["x_H2"], st["x_CO"], ray, dirs, cell_size)
     b_dop = np.sqrt(2.0 * k_boltz * np.mean(st["T_gas"]) / m_H2) / 1e5
     update_dust(st, tables)
     a_cp = 4.67e-12 * np.power(st["T_gas"] / 300.0, -0.6)

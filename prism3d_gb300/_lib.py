@@ -56,6 +56,8 @@ SIGNATURES = {
     "p3d_steady_get": [_vp, ctypes.c_int, _D],
     "p3d_steady_get_ray": [_vp, _I32],
     "p3d_steady_columns": [_vp, _D, _D],
+    "p3d_steady_dust_step": [_vp],
+    "p3d_steady_set_point_source": [_vp, _D, _f64],
     "p3d_steady_set": [_vp, ctypes.c_int, _D],
     "p3d_steady_history": [_vp, _D, _i64, _I64],
     "p3d_steady_destroy": [_vp],

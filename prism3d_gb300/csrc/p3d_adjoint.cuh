@@ -19,8 +19,12 @@
 // coefficients (SteadyParams::rs order) and log G0 (every G0-proportional
 // per-cell quantity, the dust temperature and the PE heating follow).
 //
-// Local derivatives: central differences of the FP64 residual with relative
-// steps 1e-6 (state, columns, b) and 1e-6 absolute in log parameters.  Where
+// Local derivatives: the chemistry rows' derivatives with respect to the
+// five abundances are chem5_eval's analytic Jacobian (p3d_newton.cuh); the
+// thermal row, the T column and the derivatives with respect to the
+// columns, b and the log parameters are central differences of the FP64
+// residual with relative steps 1e-6 (state, columns, b) and 1e-6 absolute in
+// log parameters.  Where
 // the outer map T -> selected thermal root is discontinuous (the forward
 // iteration converges onto the discontinuity) the thermal row is the
 // condition that pins T there: a bisection decision of the root selection
@@ -72,7 +76,8 @@ __device__ __forceinline__ AdjStatic adj_static(const SteadyDev& d, int64_t i) {
 __device__ void adj_residual(int64_t i, const SteadyDev& d, const SteadyParams& p,
                              const double* __restrict__ a_nano, const double* __restrict__ a_rest,
                              const double* u, double n2, double n3, double b, const double* th,
-                             double t_eval, const AdjStatic& st, double* G) {
+                             double t_eval, const AdjStatic& st, double* G,
+                             double (*jchem)[5] = nullptr) {
   const double nh = st.nh;
   const double T = u[5];
   const double gs = exp(th[8]);
@@ -91,7 +96,7 @@ __device__ void adj_residual(int64_t i, const SteadyDev& d, const SteadyParams& 
   const double zeta = cr_rate(st.nhc, p.zeta0);
   const double xe = fmax(u[2] + p.x_hcop, 1e-30);
   const double td = tdust(tdust_rad(g0, av), nh, T);
-  const double rh2 = h2_form(T, td, p.f_nano, p.sigma_nano, p.sigma_lc, p.sigma_sil);
+  const double rh2 = h2_form(T, td, d.f_nano[i], p.sigma_nano, p.sigma_lc, p.sigma_sil);
   ChemCell cc;
   cc.n_h = nh;
   cc.kci = kci * m[3];
@@ -113,10 +118,15 @@ __device__ void adj_residual(int64_t i, const SteadyDev& d, const SteadyParams& 
   chem5_eval(cc, u, f, J, sc, &fh2);
 #pragma unroll
   for (int k = 0; k < 5; ++k) G[k] = f[k];
+  if (jchem)
+#pragma unroll
+    for (int r = 0; r < 5; ++r)
+#pragma unroll
+      for (int c = 0; c < 5; ++c) jchem[r][c] = J[r][c];
   const double x0 = u[0], x1 = u[1], x3 = u[3];
   ThermalCtx c;
   const double uv = uv0 * fh2;
-  double gf = pe_cell(p.pe, a_nano, a_rest, g0, T, xe, nh, p.f_nano, p.e_g);
+  double gf = pe_cell(p.pe, a_nano, a_rest, g0, T, xe, nh, d.f_nano[i], d.e_g[i]);
   gf += 3.3e-11 * uv * x1 * nh * (0.4 * kEVtoErg);
   gf += rh2 * x0 * (nh * nh) * (1.5 * kEVtoErg);
   gf += 3.0e-10 * uv * x1 * nh * (2.0 * kEVtoErg) * (nh / (nh + 3e4));
@@ -179,8 +189,8 @@ adj_local_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restric
     double th[kAdjParams];
 #pragma unroll
     for (int k = 0; k < kAdjParams; ++k) th[k] = 0.0;
-    double G0[6], Gp[6], Gm[6];
-    adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b, th, -1.0, st, G0);
+    double G0[6], Gp[6], Gm[6], Jc[5][5];
+    adj_residual(i, d, p, a_nano, a_rest, u, n2, n3, b, th, -1.0, st, G0, Jc);
     // Thermal row.  A smooth root: net_heating(T) = 0.  Otherwise the outer
     // map T -> selected root is discontinuous at T: either the net heating
     // itself jumps there (T held: dT = 0), or one of the ten bisection
@@ -225,6 +235,11 @@ adj_local_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restric
       adj_residual(i, d, p, a_nano, a_rest, um, n2, n3, b, th, t_eval, st, Gm);
       for (int r = 0; r < 6; ++r) J[r][k] = (Gp[r] - Gm[r]) / (2.0 * h);
     }
+    // the chemistry block is exact: chem5_eval's analytic Jacobian (the
+    // differences above supply the thermal row and the T column, which have
+    // no closed form here)
+    for (int r = 0; r < 5; ++r)
+      for (int c = 0; c < 5; ++c) J[r][c] = Jc[r][c];
     // columns, Doppler parameter, log parameters
     double jn2[6], jn3[6], jb[6], jth[6 * kAdjParams];
     {

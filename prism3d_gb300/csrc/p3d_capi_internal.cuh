@@ -35,6 +35,15 @@ int cuda_fail(cudaError_t e, const char* where);
 int get_state(DeviceState** out);
 int sync_check(cudaStream_t s, const char* where);
 void co_ladder_host(CoLevel* out);
+// One THEMIS grain step (f_nano, E_g in place) per cell, p3d_dust.cu.
+cudaError_t launch_dust_evolve(int64_t n, const double* g0, const double* nh, double* f_nano,
+                               double* e_g, int sms, cudaStream_t s);
+// FUV field of a point source (p3d_point_source.cu); cols_only = 1 writes
+// N_H2 / N_CO only.
+cudaError_t launch_point_source(int64_t nx, int64_t ny, int64_t nz, const double* dens,
+                                const double* xh2, const double* xco, const double* star_pos,
+                                double lum, double cell, int cols_only, double* g0, double* av,
+                                double* nh, double* nh2, double* nco, int sms, cudaStream_t s);
 int build_rayset(const double* dirs, const double* weights, int64_t n_rays,
                  const double* g0_ext, int64_t n_g0, double cell_size, RaySet* rs);
 

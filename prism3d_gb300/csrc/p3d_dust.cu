@@ -30,6 +30,13 @@ __global__ void dust_evolve_kernel(int64_t n, const double* __restrict__ g0,
   }
 }
 
+cudaError_t launch_dust_evolve(int64_t n, const double* g0, const double* nh, double* f_nano,
+                               double* e_g, int sms, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  dust_evolve_kernel<<<grid_for(n, sms, 8), kThreads, 0, s>>>(n, g0, nh, f_nano, e_g);
+  return cudaGetLastError();
+}
+
 }  // namespace p3d
 
 using namespace p3d;

@@ -30,6 +30,7 @@ struct PsGeom {
   int64_t star[3];
   double spos[3];
   double cell, lum;
+  int cols_only;  // 1: write N_H2 / N_CO only (the steady driver's per-iteration columns)
 };
 
 __device__ __forceinline__ void ps_cell(const PsGeom& g, int axis, int64_t c, const int64_t* idx,
@@ -54,14 +55,15 @@ __device__ __forceinline__ void ps_cell(const PsGeom& g, int axis, int64_t c, co
       fmax(__dsub_rn(__dmul_rn(col_h2, pc), __dmul_rn(__dmul_rn(0.5, lay_h2), pc)), 0.0);
   const double tco =
       fmax(__dsub_rn(__dmul_rn(col_co, pc), __dmul_rn(__dmul_rn(0.5, lay_co), pc)), 0.0);
+  nh2[c] = th2;
+  nco[c] = tco;
+  if (g.cols_only) return;
   const double a = __dmul_rn(th, kAVperNH);
   const double four_pi = 4.0 * 3.14159265358979323846;
   const double unatt = g.lum / __dmul_rn(__dmul_rn(four_pi, __dmul_rn(r, r)), kG0ToFlux);
   g0[c] = unatt * exp(-1.8 * a);
   av[c] = a;
   nh[c] = th;
-  nh2[c] = th2;
-  nco[c] = tco;
 }
 
 __global__ void point_source_kernel(int axis, PsGeom g, const double* __restrict__ dens,
@@ -124,6 +126,27 @@ static int64_t star_index(double pos, double cell, int64_t n) {
   return (int64_t)v;  // truncation, as int() of the clipped value
 }
 
+cudaError_t launch_point_source(int64_t nx, int64_t ny, int64_t nz, const double* dens,
+                                const double* xh2, const double* xco, const double* star_pos,
+                                double lum, double cell, int cols_only, double* g0, double* av,
+                                double* nh, double* nh2, double* nco, int sms, cudaStream_t s) {
+  PsGeom g;
+  g.n[0] = nx; g.n[1] = ny; g.n[2] = nz;
+  g.cell = cell;
+  g.lum = lum;
+  g.cols_only = cols_only;
+  for (int k = 0; k < 3; ++k) {
+    g.spos[k] = star_pos[k];
+    g.star[k] = star_index(star_pos[k], cell, g.n[k]);
+  }
+  for (int axis = 0; axis < 3; ++axis) {
+    const int a1 = axis == 0 ? 1 : 0, a2 = axis == 2 ? 1 : 2;
+    point_source_kernel<<<grid_for(g.n[a1] * g.n[a2], sms, 8), kThreads, 0, s>>>(
+        axis, g, dens, xh2, xco, g0, av, nh, nh2, nco);
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace p3d
 
 using namespace p3d;
@@ -141,21 +164,9 @@ int p3d_fuv_point_source_dev(int64_t nx, int64_t ny, int64_t nz, const double* d
   if (!(cell_size > 0.0)) return set_error(P3D_EINVAL, "cell_size must be > 0");
   if (!density || !star_pos || !g0 || !a_v || !n_h || !n_h2 || !n_co)
     return set_error(P3D_EINVAL, "null array");
-  PsGeom g;
-  g.n[0] = nx; g.n[1] = ny; g.n[2] = nz;
-  g.cell = cell_size;
-  g.lum = L_fuv;
-  for (int k = 0; k < 3; ++k) {
-    g.spos[k] = star_pos[k];
-    g.star[k] = star_index(star_pos[k], cell_size, g.n[k]);
-  }
-  cudaStream_t s = (cudaStream_t)stream;
-  for (int axis = 0; axis < 3; ++axis) {
-    const int a1 = axis == 0 ? 1 : 0, a2 = axis == 2 ? 1 : 2;
-    point_source_kernel<<<grid_for(g.n[a1] * g.n[a2], st->sms, 8), kThreads, 0, s>>>(
-        axis, g, density, x_h2, x_co, g0, a_v, n_h, n_h2, n_co);
-  }
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_point_source(nx, ny, nz, density, x_h2, x_co, star_pos, L_fuv,
+                                      cell_size, 0, g0, a_v, n_h, n_h2, n_co, st->sms,
+                                      (cudaStream_t)stream);
   return e == cudaSuccess ? P3D_OK : cuda_fail(e, "point source launch");
 }
 

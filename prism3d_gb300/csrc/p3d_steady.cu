@@ -26,7 +26,12 @@ constexpr int kMaxHist = 1 << 16;
 struct SteadySolver {
   DeviceState* st = nullptr;
   int64_t nx = 0, ny = 0, nz = 0, n = 0;
+  double cell = 0.0;
   RaySet rays;
+  // point source (solver_3d.py:270-276): the field and the per-iteration
+  // H2 / CO columns come from the star instead of the external ray set
+  int star = 0;
+  double star_pos[3] = {0.0, 0.0, 0.0}, star_lum = 0.0;
   SteadyParams par;
   SteadyDev d;
   std::vector<void*> allocs;
@@ -87,6 +92,11 @@ static unsigned cell_grid(int64_t n, int sms, int threads, int per_sm) {
 // of each axis per pencil read (ss_columns_kernel).
 static void launch_columns(SteadySolver* s, const SteadyParams& par, cudaStream_t str) {
   const SteadyDev& d = s->d;
+  if (s->star) {  // columns towards the star (the cell's own half layer included)
+    launch_point_source(s->nx, s->ny, s->nz, s->dens, d.x_h2, d.x_co, s->star_pos, s->star_lum,
+                        s->cell, 1, nullptr, nullptr, nullptr, d.u_h2, d.u_co, s->st->sms, str);
+    return;
+  }
   const ColumnsGrid g = columns_grid(s->nx, s->ny, s->nz);
   ss_columns_kernel<<<(unsigned)(g.nbx + g.nby + g.nbz), 32 * kColWarps,
                       columns_smem_bytes(s->nx, s->ny), str>>>(
@@ -116,7 +126,12 @@ static int launch_iteration(SteadySolver* s, bool mixed, const SteadyParams& par
   return e == cudaSuccess ? P3D_OK : cuda_fail(e, "steady iteration launch");
 }
 
-constexpr int kLaunchesPerIteration = 7;  // mixed; the plain path launches 6
+// kernels of one mixed iteration with the ray-set columns (the plain path
+// launches one fewer; the point-source columns take three launches, not one)
+constexpr int kLaunchesPerIteration = 7;
+static int launches_per_iteration(const SteadySolver* s, bool mixed) {
+  return kLaunchesPerIteration - (mixed ? 0 : 1) + (s->star ? 2 : 0);
+}
 
 }  // namespace p3d
 
@@ -152,6 +167,7 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   s->st = st;
   s->nx = nx; s->ny = ny; s->nz = nz; s->n = nx * ny * nz;
   const int64_t n = s->n;
+  s->cell = cell_size;
   if ((rc = build_rayset(dirs, weights, n_rays, g0_ext, n_g0, cell_size, &s->rays))) {
     delete h;
     return rc;
@@ -177,7 +193,7 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   SteadyDev& d = s->d;
   double** dbl[] = {&s->dens, &d.g0, &d.av, &d.nh_col, &s->nh2_full, &s->nco_full, &d.ds,
                     &d.kpd0, &d.uv0, &d.kci, &d.kco0, &d.hci0, &d.zeta, &d.td_rad, &d.t_gas,
-                    &d.x_hi, &d.x_h2, &d.x_cp, &d.x_c, &d.x_co, &d.x_o, &d.x_e, &d.l2, &d.l3, &d.u_h2,
+                    &d.x_hi, &d.x_h2, &d.x_cp, &d.x_c, &d.x_co, &d.x_o, &d.x_e, &d.l2, &d.l3, &d.f_nano, &d.e_g, &d.u_h2,
                     &d.u_co, &d.t_prev, &d.r_prev, &d.t_lo, &d.t_hi, &d.span, &d.t_root, &d.u_h2_last, &d.u_co_last, &d.b_last, &d.chg_last, &d.rh2_cell, &d.chg_spec, &d.fh2,
                     &d.gamma_pe, &d.t_dust, &s->scratch};
   for (double** q : dbl)
@@ -289,12 +305,20 @@ int p3d_steady_reset(p3d_steady_t* h) {
     cudaEventCreate(&s->ev_stop);
   }
   cudaEventRecord(s->ev_start, str);
+  cudaError_t e;
+  if (s->star) {
+    e = launch_point_source(s->nx, s->ny, s->nz, s->dens, nullptr, nullptr, s->star_pos,
+                            s->star_lum, s->cell, 0, d.g0, d.av, d.nh_col, s->nh2_full,
+                            s->nco_full, s->st->sms, str);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.ray, 0xff, sizeof(int32_t) * s->n, str);
+  } else {
   int err = 0;
   void* work = s->st->slot(kSlotRtWork, rt_work_bytes(s->n), &err);
   if (err) return err;
-  cudaError_t e = launch_fuv_full(s->nx, s->ny, s->nz, s->dens, nullptr, nullptr, s->rays, work, d.g0,
+  e = launch_fuv_full(s->nx, s->ny, s->nz, s->dens, nullptr, nullptr, s->rays, work, d.g0,
                                   d.av, d.nh_col, s->nh2_full, s->nco_full, d.ray, s->st->sms,
                                   str);
+  }
   if (e != cudaSuccess) return cuda_fail(e, "reset: ray march");
   ss_setup_kernel<<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(s->n, d, s->par,
                                                                         s->ray_ds, s->ray_fam);
@@ -304,7 +328,7 @@ int p3d_steady_reset(p3d_steady_t* h) {
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "reset launch");
   s->iters_done = 0;
-  s->launches = rt_launch_count(s->rays) + 2;  // ray march, setup, globals
+  s->launches = (s->star ? 3 : rt_launch_count(s->rays)) + 2;  // ray march, setup, globals
   s->last_dmax = INFINITY;
   return P3D_OK;
 }
@@ -352,7 +376,7 @@ int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, in
                           sizeof(double) * kHistCols, cudaMemcpyDeviceToHost, str);
       if (e == cudaSuccess) e = cudaStreamSynchronize(str);
       if (e != cudaSuccess) return cuda_fail(e, "plain iteration");
-      s->launches += kLaunchesPerIteration - (mixed ? 0 : 1);
+      s->launches += launches_per_iteration(s, mixed != 0);
       s->last_dmax = s->hist_host[kHistCols * it];
       bool c = conv(s->hist_host + kHistCols * it);
       ++it;
@@ -380,21 +404,20 @@ int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, in
     while (it < stop && !done) {
       if (it + kGraphIters > kMaxHist) return set_error(P3D_EINVAL, "iteration history full");
       e = cudaGraphLaunch(s->graph, str);
-      s->launches += (int64_t)kLaunchesPerIteration * kGraphIters;
+      s->launches += (int64_t)launches_per_iteration(s, true) * kGraphIters;
       if (e == cudaSuccess)
         e = cudaMemcpyAsync(s->hist_host + kHistCols * it, s->hist + kHistCols * it,
                             sizeof(double) * kHistCols * kGraphIters, cudaMemcpyDeviceToHost, str);
       if (e == cudaSuccess) e = cudaStreamSynchronize(str);
       if (e != cudaSuccess) return cuda_fail(e, "mixed graph launch");
-      for (int k = 0; k < kGraphIters; ++k) {
-        s->last_dmax = s->hist_host[kHistCols * (it + k)];
-        if (conv(s->hist_host + kHistCols * (it + k)) && it + k + 1 > 2) {
-          done = true;
-          it += k + 1;
-          break;
-        }
-      }
-      if (!done) it += kGraphIters;
+      // the device ran all kGraphIters iterations: count them all (the
+      // history rows and the device's iteration counter stay in step with
+      // the host's, which a later run() after a dust step relies on) and
+      // test convergence on the batch's last iteration, the state returned
+      const double* last = s->hist_host + kHistCols * (it + kGraphIters - 1);
+      s->last_dmax = last[0];
+      it += kGraphIters;
+      if (conv(last) && it > 2) done = true;
     }
   }
   s->iters_done = it;
@@ -438,6 +461,8 @@ int p3d_steady_get(p3d_steady_t* h, int field, double* host_out) {
     case P3D_F_ZETA: src = d.zeta; break;
     case P3D_F_F_SH_H2: src = d.fh2; break;
     case P3D_F_CHANGE: src = d.chg_last; break;
+    case P3D_F_F_NANO: src = d.f_nano; break;
+    case P3D_F_E_G: src = d.e_g; break;
     case P3D_F_GAMMA:
     case P3D_F_LAMBDA:
       ss_heating_cooling_kernel<<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(
@@ -458,6 +483,41 @@ int p3d_steady_get(p3d_steady_t* h, int field, double* host_out) {
                                   str);
   if (e == cudaSuccess) e = cudaStreamSynchronize(str);
   return e == cudaSuccess ? P3D_OK : cuda_fail(e, "steady get");
+}
+
+int p3d_steady_set_point_source(p3d_steady_t* h, const double* star_pos, double l_fuv) {
+  if (!h) return set_error(P3D_EINVAL, "null handle");
+  SteadySolver* s = &h->s;
+  if (!(l_fuv > 0.0)) {
+    s->star = 0;
+    return P3D_OK;
+  }
+  if (!star_pos) return set_error(P3D_EINVAL, "null star position");
+  if (s->par.h2_implicit)
+    return set_error(P3D_EINVAL, "the point-source columns include the cell's own layer");
+  s->star = 1;
+  for (int k = 0; k < 3; ++k) s->star_pos[k] = star_pos[k];
+  s->star_lum = l_fuv;
+  if (s->graph) {  // the captured iterations hold the other columns launch
+    cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+  }
+  return P3D_OK;
+}
+
+int p3d_steady_dust_step(p3d_steady_t* h) {
+  if (!h) return set_error(P3D_EINVAL, "null handle");
+  SteadySolver* s = &h->s;
+  cudaStream_t str = s->st->stream;
+  cudaError_t e = launch_dust_evolve(s->n, s->d.g0, s->dens, s->d.f_nano, s->d.e_g, s->st->sms,
+                                     str);
+  if (e == cudaSuccess) {
+    ss_dust_restart_kernel<<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(s->n, s->d);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "dust step launch");
+  s->launches += 2;
+  return P3D_OK;
 }
 
 int p3d_steady_columns(p3d_steady_t* h, double* nh2_out, double* nco_out) {
@@ -716,6 +776,8 @@ int p3d_steady_adjoint(p3d_steady_t* h, const double* w6, double dx, int64_t max
     return set_error(P3D_EINVAL, "max_sweeps >= 1, tol > 0, dx > 0, 0 < omega <= 1 required");
   SteadySolver* s = &h->s;
   if (s->iters_done < 1) return set_error(P3D_EINVAL, "run the steady state before its adjoint");
+  if (s->star)
+    return set_error(P3D_EINVAL, "the adjoint covers the external ray-set field, not a point source");
   cudaStream_t str = s->st->stream;
   const int64_t n = s->n;
   const SteadyDev& d = s->d;

@@ -15,6 +15,9 @@ struct SteadyDev {
   int32_t* ray;
   double *ds, *kpd0, *uv0, *kci, *kco0, *hci0, *zeta, *td_rad;
   int8_t* fam;  // selected ray family: axis * 2 + (1 if cumsum ascends)
+  // THEMIS grain state per cell (nano-grain fraction, band gap): the
+  // reference's initial values at reset, then one grain step per dust step
+  double *f_nano, *e_g;
   // state
   double *t_gas, *x_hi, *x_h2, *x_cp, *x_c, *x_co, *x_o, *x_e;
   // column layers of the current abundances, 2 n x_H2 and n x_CO (kept by

@@ -80,6 +80,25 @@ __global__ void ss_layers_kernel(int64_t n, SteadyDev d) {
   }
 }
 
+// After a grain step every cell's PE heating and H2 formation change, so
+// the fixed point moves: forget the last solve's change (the worklist solves
+// every cell again), its bisection decisions (the root's inputs moved in a
+// way the replay test does not see) and the T-update brackets, as the
+// reference restarts its per-cell damping for every dust step
+// (solver_3d.py:252-254).  State and warm-start roots are kept.
+__global__ void ss_dust_restart_kernel(int64_t n, SteadyDev d) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    d.chg_last[i] = INFINITY;
+    d.bis_node[i] = 0;
+    d.t_prev[i] = 0.0;
+    d.r_prev[i] = 0.0;
+    d.t_lo[i] = 0.0;
+    d.t_hi[i] = INFINITY;
+    d.span[i] = INFINITY;
+  }
+}
+
 // ----------------------------------------------------------------- setup
 __global__ void __launch_bounds__(kThreads)
 ss_setup_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restrict__ ray_ds,
@@ -124,6 +143,8 @@ ss_setup_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* __restrict
     d.x_o[i] = fmax(p.x_o_total - xco, 1e-10);
     d.x_e[i] = fmax(xcp + p.x_hcop, 1e-10);
     d.t_gas[i] = p.t_init;
+    d.f_nano[i] = p.f_nano;
+    d.e_g[i] = p.e_g;
     d.t_prev[i] = 0.0;
     d.r_prev[i] = 0.0;
     d.t_lo[i] = 0.0;
@@ -528,9 +549,10 @@ ss_chem_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g,
     const double xe0 = d.x_e[i];
     double y_old[5] = {d.x_hi[i], d.x_h2[i], d.x_cp[i], d.x_c[i], d.x_co[i]};
     // dust coupling at the current T (solver_3d.py:509-530)
-    const double gpe = pe_cell(p.pe, a_nano, a_rest, d.g0[i], tg, xe0, nh, p.f_nano, p.e_g);
+    const double fn = d.f_nano[i];
+    const double gpe = pe_cell(p.pe, a_nano, a_rest, d.g0[i], tg, xe0, nh, fn, d.e_g[i]);
     const double td = tdust(d.td_rad[i], nh, tg);
-    const double rh2 = h2_form(tg, td, p.f_nano, p.sigma_nano, p.sigma_lc, p.sigma_sil);
+    const double rh2 = h2_form(tg, td, fn, p.sigma_nano, p.sigma_lc, p.sigma_sil);
     const double zeta = d.zeta[i];
     // chemistry (solver_3d.py:549-557 rates; steady state of chemistry.rs:35-49)
     ChemCell cc;
@@ -837,9 +859,10 @@ ss_refine_scatter_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* _
     d.l2[i] = col_layer_h2(nh, x1);
     d.l3[i] = col_layer_co(nh, x[kNetCO]);
     const double tg = d.t_gas[i];
-    const double gpe = pe_cell(p.pe, a_nano, a_rest, d.g0[i], tg, xe, nh, p.f_nano, p.e_g);
+    const double fn = d.f_nano[i];
+    const double gpe = pe_cell(p.pe, a_nano, a_rest, d.g0[i], tg, xe, nh, fn, d.e_g[i]);
     const double td = tdust(d.td_rad[i], nh, tg);
-    const double rh2 = h2_form(tg, td, p.f_nano, p.sigma_nano, p.sigma_lc, p.sigma_sil);
+    const double rh2 = h2_form(tg, td, fn, p.sigma_nano, p.sigma_lc, p.sigma_sil);
     const double zeta = d.zeta[i];
     const double uv = d.uv0[i] * d.fh2[i];
     ThermalCtx c;

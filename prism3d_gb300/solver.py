@@ -27,7 +27,8 @@ from .tables import DustTables, line_params
 
 FIELDS = {"T_gas": 0, "x_HI": 1, "x_H2": 2, "x_Cp": 3, "x_C": 4, "x_CO": 5, "x_O": 6, "x_e": 7,
           "G0": 8, "A_V": 9, "N_H": 10, "N_H2": 11, "N_CO": 12, "T_dust": 13, "Gamma_PE": 14,
-          "zeta_CR": 15, "f_sh_H2": 16, "Gamma": 17, "Lambda": 18, "change": 19}
+          "zeta_CR": 15, "f_sh_H2": 16, "Gamma": 17, "Lambda": 18, "change": 19, "f_nano": 20,
+          "E_g": 21}
 
 
 class NotConvergedError(RuntimeError):
@@ -38,7 +39,7 @@ class PDRSolverGPU:
     """Device-resident PRISM-3D steady state on one GB300."""
 
     def __init__(self, density, box_size, G0_external=1.0, zeta_CR_0=2e-16, nside_rt=1,
-                 T_init=50.0, tables=None):
+                 T_init=50.0, tables=None, star=None):
         self.density = np.ascontiguousarray(density, dtype=np.float64)
         if self.density.ndim != 3:
             raise ValueError("density must be (nx, ny, nz)")
@@ -68,6 +69,13 @@ class PDRSolverGPU:
                tb.log_psi_step, tb.n_psi, tb.eg_min, tb.eg_step, tb.n_Eg,
                p(tb.bin_sigma_abs), p(tb.bin_dn_da_da), p(tb.bin_is_nano.astype(np.float64)),
                p(sig), *[p(a) for a in lines])
+        # point source: dict with 'position' [cm] and 'L_FUV' [erg/s], as the
+        # reference's PDRSolver3D(star=...) (solver_3d.py:70-71, 270-276)
+        self.star = star
+        if star is not None:
+            self._star_pos = np.ascontiguousarray(star["position"], dtype=np.float64).reshape(3)
+            L.call("p3d_steady_set_point_source", self._h, p(self._star_pos),
+                   float(star["L_FUV"]))
         self.reset()
 
     def reset(self):
@@ -76,10 +84,26 @@ class PDRSolverGPU:
         self.iterations = 0
 
     def run(self, max_iterations=2000, convergence_tol=1e-8, mixed=True, w_chem=0.5, w_T=0.5,
-            n_allow=None, raise_on_failure=False):
+            n_allow=None, raise_on_failure=False, dust_steps=1):
         """Outer iterations until at most n_allow cells (default
         max(8, 1e-5 n_cells)) change by more than convergence_tol (relative,
-        T_gas and species above 1e-20).  Returns True when converged."""
+        T_gas and species above 1e-20).  With dust_steps > 1 the reference's
+        two-level loop (solver_3d.py:239-249): before every inner
+        convergence but the first, one THEMIS grain step (_evolve_dust_state)
+        on every cell; max_iterations bounds each inner loop.  Returns True
+        when the (last) inner loop converged."""
+        if dust_steps < 1:
+            raise ValueError("dust_steps must be >= 1")
+        ok = True
+        for step in range(int(dust_steps)):
+            if step > 0:
+                L.call("p3d_steady_dust_step", self._h)
+            ok = self._inner(max_iterations, convergence_tol, mixed, w_chem, w_T, n_allow,
+                             raise_on_failure)
+        return ok
+
+    def _inner(self, max_iterations, convergence_tol, mixed, w_chem, w_T, n_allow,
+               raise_on_failure):
         if n_allow is None:
             n_allow = max(8, int(1e-5 * self.n_cells))
         it = L._i64(0)
@@ -252,8 +276,7 @@ class PDRSolverGPU:
             x_C=st["x_C"], x_CO=st["x_CO"], x_O=st["x_O"], x_e=st["x_e"],
             x_OH=1e-9 + 9e-8 * np.clip(10.0 * st["x_H2"], 0, 1), x_H2O=np.full(shp, 1e-8),
             x_HCOp=np.full(shp, 1e-10), Gamma=st["Gamma"], Lambda=st["Lambda"],
-            Gamma_PE=st["Gamma_PE"], f_nano=np.ones(shp),
-            E_g=np.full(shp, 0.1), box_size=self.box_size,
+            Gamma_PE=st["Gamma_PE"], f_nano=st["f_nano"], E_g=st["E_g"], box_size=self.box_size,
             G0_external=np.max(np.atleast_1d(self.G0_external)), zeta_CR_0=self.zeta_CR_0,
             G0_rays=np.atleast_1d(np.asarray(self.G0_external, dtype=np.float64)),
             nside_rt=self.nside_rt)

@@ -52,6 +52,37 @@ extern "C" void hc_chem_steady(long n, const double* n_h, const double* kpd0,
   }
 }
 
+// Residual f (5) and analytic Jacobian J (5 x 5, row-major) of the reduced
+// chemistry at one state (chem5_eval, the rows the adjoint's per-cell
+// Jacobian takes), with the shielding fixed by the columns (ds = 0, as in the
+// adjoint) or with the cell's own H2 half layer inside (ds > 0).
+extern "C" void hc_chem5_eval(double n_h, double kpd0, double kci, double acp, double kco0,
+                              double rh2_half_nh, double rcr, double x_c_total, double x_hcop,
+                              double kco_cr, double koh_s, double u_h2, double u_co,
+                              double ds, double b_dop, const double* y, double* f, double* J) {
+  ChemCell cc;
+  cc.n_h = n_h;
+  cc.kci = kci;
+  cc.acp = acp;
+  cc.rh2 = rh2_half_nh;
+  cc.rcr = rcr;
+  cc.xc = x_c_total;
+  cc.hcop = x_hcop;
+  cc.kpd0 = kpd0;
+  cc.kco0 = kco0;
+  cc.kco_cr = kco_cr;
+  cc.koh_s = koh_s;
+  cc.u_h2 = u_h2;
+  cc.u_co = u_co;
+  cc.ds = ds;
+  cc.b_dop = b_dop;
+  chem_prepare(cc);
+  double Jm[5][5], sc[5], fh2;
+  chem5_eval(cc, y, f, Jm, sc, &fh2);
+  for (int r = 0; r < 5; ++r)
+    for (int c = 0; c < 5; ++c) J[5 * r + c] = Jm[r][c];
+}
+
 // H2 self-shielding factor and the slope the steady driver's worklist keeps
 // (|d ln f_H2 / d ln b|), for the CPU tests.
 extern "C" void hc_fsh_h2(long n, const double* nh2, const double* b, double* f,

@@ -126,3 +126,53 @@ def test_shielding_slope_in_doppler_width(lib):
     # the kernel's f_H2 is the reference's f_shield_H2 with b = sqrt(2 k T / m_H2) / 1e5
     T = (b * 1e5) ** 2 * O.m_H2 / (2.0 * O.k_boltz)
     np.testing.assert_allclose(f, O.f_shield_H2(nh2, T), rtol=1e-12)
+
+
+def test_analytic_jacobian_matches_fp64_differences(lib):
+    """chem5_eval's analytic Jacobian (the chemistry block of the adjoint's
+    per-cell Jacobian, p3d_adjoint.cuh) against central differences of the
+    same FP64 residual on seeded states over the PDR range, with the
+    shielding fixed by the columns and with the cell's own H2 half layer
+    inside the solve.  The allowed difference is the difference quotient's
+    own error: 1e-6 of the entry (truncation) plus the rounding of the
+    residual's terms over the step."""
+    rng = np.random.default_rng(17)
+    dbl = ctypes.c_double
+    worst = 0.0
+    for trial in range(400):
+        nh = 10 ** rng.uniform(1, 6.5)
+        g0 = 10 ** rng.uniform(-1, 5)
+        av = rng.uniform(0, 10)
+        zeta = 10 ** rng.uniform(-17, -15)
+        T = 10 ** rng.uniform(1, 4)
+        kpd0 = 4.43e-11 * g0 * np.exp(-3.74 * av)
+        kci = 2.56e-10 * g0 * np.exp(-3.02 * av)
+        kco0 = 1.71e-10 * g0 * np.exp(-3.53 * av)
+        acp = 4.67e-12 * (T / 300.0) ** -0.6
+        rh2 = 10 ** rng.uniform(-18, -16) * nh * 0.5
+        xh2 = rng.uniform(1e-6, 0.49)
+        y = np.array([1 - 2 * xh2, xh2, 10 ** rng.uniform(-9, -4.1), 10 ** rng.uniform(-9, -4.1),
+                      10 ** rng.uniform(-12, -4.1)])
+        u_h2 = 10 ** rng.uniform(12, 22)
+        u_co = 10 ** rng.uniform(8, 18)
+        ds = 0.0 if trial % 2 == 0 else 1.5e16
+        args = [dbl(v) for v in (nh, kpd0, kci, acp, kco0, rh2, 0.25 * zeta, 1.076e-4, 1e-10,
+                                 6 * zeta, 1.0, u_h2, u_co, ds, 1.2)]
+        f = np.zeros(5)
+        J = np.zeros(25)
+        lib.hc_chem5_eval(*args, _p(np.ascontiguousarray(y)), _p(f), _p(J))
+        J = J.reshape(5, 5)
+        terms = np.abs(J) @ np.abs(y) + np.abs(f)
+        for c in range(5):
+            h = 1e-6 * y[c]
+            fp, fm, junk = np.zeros(5), np.zeros(5), np.zeros(25)
+            yp, ym = y.copy(), y.copy()
+            yp[c] += h
+            ym[c] -= h
+            lib.hc_chem5_eval(*args, _p(yp), _p(fp), _p(junk))
+            lib.hc_chem5_eval(*args, _p(ym), _p(fm), _p(junk))
+            fd = (fp - fm) / (2 * h)
+            for r in range(5):
+                allowed = 1e-6 * abs(J[r, c]) + 8 * 2.2e-16 * terms[r] / (2 * h)
+                worst = max(worst, abs(J[r, c] - fd[r]) / allowed)
+    assert worst < 1.0, worst

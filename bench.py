@@ -237,7 +237,7 @@ def run_gb300(args, ws, rank, local):
     kt = kernel_times(s, reps=1)
     hbm, peak_kind = measured_peaks()
     fp64_peak = fp64_peak_tflops()
-    col_bytes = 49.0 * n  # read n_H, x_H2, x_CO, ds, family once; write N_H2, N_CO
+    col_bytes = 41.0 * n  # read layers 2 n x_H2, n x_CO, family, ds once; write N_H2, N_CO
     col_gbs = col_bytes / (kt["columns_ms"] * 1e-3) / 1e9
     cell_tf = FP64_OPS_PER_CELL_SOLVE * n / (kt["cell_mixed_ms"] * 1e-3) / 1e12
     out = {
@@ -271,13 +271,17 @@ def run_gb300(args, ws, rank, local):
                      "per_unit": f"{FP64_OPS_PER_CELL_SOLVE:.0f} FP64 flops per cell solve "
                                  "(ncu DADD + DMUL + 2 DFMA counts of the two kernels)",
                      "fp32_flops_per_cell_solve": FP32_OPS_PER_CELL_SOLVE,
-                     "counts_commit": COUNTS_COMMIT,
+                     "counts_source": "profiles/cell_kernels_slab128.md",
                      "fp64_pipe_active_ncu": FP64_PIPE_ACTIVE_NCU},
-        "roofline_hbm": {"kernel": "ss_columns_all_kernel (3 axes x 2 directions, one launch per "
+        "roofline_hbm": {"kernel": "ss_columns_kernel (3 axes x 2 directions, one launch per "
                                    "outer iteration)",
                          "bound": "hbm", "achieved": col_gbs, "peak": hbm, "unit": "GB/s",
-                         "frac": col_gbs / hbm, "traffic": None, "peak_source": peak_kind,
-                         "algorithmic_bytes_per_launch": col_bytes},
+                         "frac": col_gbs / hbm, "traffic": COLUMNS_DRAM_BYTES_PER_CELL * n,
+                         "peak_source": peak_kind, "algorithmic_bytes_per_launch": col_bytes,
+                         "note": "FP64-pipe bound (82% busy: 21 DADD per cell for the running "
+                                 "sums), not HBM; traffic below the algorithmic bytes: the "
+                                 "layers are partly L2-resident, the columns stay in L2 "
+                                 "(profiles/columns_rt_slab128.md)"},
         "kernel_times_ms": kt,
         "fp64_net_heating_evals_per_cell_iter": float(np.mean(hist[:, 6]) / n),
         "gpu_launches": int(sum(launches)),
@@ -299,7 +303,8 @@ def run_gb300(args, ws, rank, local):
                           "GB_per_s": 40 * n / tm / 1e9,
                           "note": "5 fields read once (n_H, x_H2, x_CO, x_C+, x_e), LOS = z, "
                                   "host clock around p3d_steady_column_maps"}
-    out["rt_dropin"] = rt_dropin_bench(dens, g0, cell, nside, outs, hbm, peak_kind)
+    out["rt_dropin"] = rt_dropin_bench(dens, g0, cell, nside, outs, hbm, peak_kind, fp64_peak,
+                                       args.workload)
     if args.production and args.workload == "slab128":
         out["production_256"] = production_bench(args)
     out["cpu_baseline"] = cpu_baseline(args, dens, g0, nside, zeta, cell, float(np.mean(iters)))
@@ -365,12 +370,15 @@ def production_bench(args):
         err[k] = {"frac_le_1e-6": float(np.mean(rel <= 1e-6)), "p99": float(np.quantile(rel, 0.99)),
                   "max": float(rel.max())}
     res["subvolume_64_mixed_vs_plain"] = err
-    res["subvolume_64_moving"] = [int(np.sum(st[True]["change"] > args.tol)),
-                                  int(np.sum(st[False]["change"] > args.tol))]
+    acc = accuracy_block([st[True][k] for k in STATE_KEYS], [st[False][k] for k in STATE_KEYS],
+                         st[True]["change"] > args.tol, st[False]["change"] > args.tol,
+                         max(8, int(1e-5 * sub.size)))
+    res["subvolume_64_accuracy"] = {k: acc[k] for k in ("cells_beyond", "cells_beyond_settled",
+                                                        "moving", "n_allow", "ok")}
     return res
 
 
-def rt_dropin_bench(dens, g0, cell, nside, state, hbm, peak_kind):
+def rt_dropin_bench(dens, g0, cell, nside, state, hbm, peak_kind, fp64_peak, workload):
     """The drop-in FUV transfer (compute_fuv_field_3d, the call the
     reference's solver makes every outer iteration) on the converged state:
     device tensors on torch's stream (CUDA events), and from NumPy arrays
@@ -398,13 +406,22 @@ def rt_dropin_bench(dens, g0, cell, nside, state, hbm, peak_kind):
         compute_fuv_field_3d(dens, g0, cell, xh2, xco, nside)
     t_host = (time.perf_counter() - t0) / 2
     gbs = 64.0 * n / (ms * 1e-3) / 1e9
-    return {"ms": ms, "cells_per_s": n / (ms * 1e-3), "e2e_cells_per_s": n / t_host,
-            "e2e_h2d_bytes": 24 * n, "e2e_d2h_bytes": 44 * n,
-            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
-                         "frac": gbs / hbm, "peak_source": peak_kind,
-                         "per_unit": "64 B per cell (read n_H, x_H2, x_CO; write G0, A_V, N_H, "
-                                     "N_H2, N_CO)"},
-            "rays": 12 * nside * nside}
+    res = {"ms": ms, "cells_per_s": n / (ms * 1e-3), "e2e_cells_per_s": n / t_host,
+           "e2e_h2d_bytes": 24 * n, "e2e_d2h_bytes": 44 * n,
+           "hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                   "peak_source": peak_kind,
+                   "per_unit": "64 B per cell (read n_H, x_H2, x_CO; write G0, A_V, N_H, N_H2, "
+                               "N_CO)"},
+           "rays": 12 * nside * nside}
+    if workload in RT_FP64_OPS_PER_CELL and nside == 2:
+        tf = RT_FP64_OPS_PER_CELL[workload] * n / (ms * 1e-3) / 1e12
+        res["roofline"] = {"bound": "fp64", "achieved": tf, "peak": fp64_peak, "unit": "TFLOP/s",
+                           "frac": tf / fp64_peak, "peak_source": "measured live: DFMA-chain "
+                           "kernel on this GPU", "traffic": RT_DRAM_BYTES_PER_CELL[workload] * n,
+                           "per_unit": f"{RT_FP64_OPS_PER_CELL[workload]:.0f} FP64 flops per cell "
+                                       "(walk + merge, 48 rays; ncu counts, "
+                                       "profiles/columns_rt_slab128.md)"}
+    return res
 
 
 def network_bench(args):
@@ -461,19 +478,27 @@ def network_bench(args):
     return res
 
 
-# FP64 flops (DFMA = 2, DADD / DMUL = 1) per cell solve of the mixed chemistry
-# and thermal kernels on the 14th outer iteration of the 96^3 slab, every
-# cell active, from ncu instruction counts (1,754 + 3,425), and their FP32
-# flops; COUNTS_COMMIT names the kernels' source the counts were taken at.
-FP64_OPS_PER_CELL_SOLVE = 5179.0
-FP32_OPS_PER_CELL_SOLVE = 495.0 + 1777.0
-COUNTS_COMMIT = "1ffd122"
-FP64_PIPE_ACTIVE_NCU = "85-87% (chemistry and thermal kernels): the pipe also runs FP64 compares, min/max and conversions"
-# DRAM bytes of ss_chem_kernel + ss_thermal_kernel per cell solved, ncu on the
-# 96^3 slab with every cell active (read + write: 117.0 + 45.7 and 208.4 +
-# 62.4 MB for 884,736 cells): the state is streamed once per solve, so the
-# traffic scales with the cells solved
-DRAM_BYTES_PER_CELL_SOLVE = (117.0 + 45.7 + 208.4 + 62.4) * 1e6 / 884736
+# Per-cell counts of the launches bench.py times for its rooflines, from ncu
+# on `bench.py --profile kernels` / `--profile rt` at 128^3 (2,097,152
+# cells; profiles/cell_kernels_slab128.md, profiles/columns_rt_slab128.md):
+# FP64 flops (DFMA = 2, DADD / DMUL = 1) per cell solve of the mixed
+# chemistry (1,827) and thermal (1,487) kernels on the 14th outer iteration,
+# every cell solved with exact roots, and their FP32 flops (757 + 5,960);
+# DRAM bytes of the two launches (read + write: 310.7 + 203.6 and 508.8 +
+# 173.8 MB): the state is streamed once per solve, so the traffic scales
+# with the cells solved.
+FP64_OPS_PER_CELL_SOLVE = 1827.3 + 1487.3
+FP32_OPS_PER_CELL_SOLVE = 757.5 + 5960.1
+DRAM_BYTES_PER_CELL_SOLVE = (310.7 + 203.6 + 508.8 + 173.8) * 1e6 / 2097152
+FP64_PIPE_ACTIVE_NCU = ("86% (chemistry), 79% (thermal): the pipe also runs FP64 compares, "
+                        "min/max and FP32<->FP64 conversions")
+# columns launch: FP64-pipe bound (82% busy), 27 FP64 flops per cell; DRAM
+# per launch (read + write) with the chemistry's layers partly L2-resident
+COLUMNS_DRAM_BYTES_PER_CELL = (55.9 + 6.0) * 1e6 / 2097152
+# drop-in ray march (walk + merge, 48 rays) at 128^3: FP64 flops per cell
+# and DRAM bytes per cell of the two launches
+RT_FP64_OPS_PER_CELL = {"slab128": 684.0 + 12.0}
+RT_DRAM_BYTES_PER_CELL = {"slab128": (233.6 + 460.8 + 344.5 + 74.4) * 1e6 / 2097152}
 STATE_KEYS = ("T_gas", "x_HI", "x_H2", "x_Cp", "x_C", "x_CO", "x_O", "x_e")
 
 
@@ -586,6 +611,48 @@ def run_reference(args, ws, rank):
                     "d2h_bytes_per_step": 0}}
 
 
+def profile_run(args):
+    """Short, deterministic runs for ncu (no autotune, no comparison solves):
+    the launches the bench line times, with nothing else around them."""
+    import torch
+
+    from prism3d_gb300 import fields
+    from prism3d_gb300.solver import PDRSolverGPU
+    torch.cuda.set_device(0)
+    dens, g0, nside, zeta, cell = fields.workload(args.workload, seed=1)
+    n = dens.size
+    s = PDRSolverGPU(dens, cell * dens.shape[0], G0_external=g0, zeta_CR_0=zeta, nside_rt=nside,
+                     T_init=100.0)
+    t, b = (int(v) for v in args.launch.split(","))
+    s.set_launch(t, b)
+    out = {"profile": args.profile, "workload": args.workload, "n_cells": n, "launch": [t, b]}
+    if args.profile == "rt":
+        # the drop-in ray march on device tensors (its work depends on the
+        # geometry, not on the abundances)
+        from prism3d_gb300.core import compute_fuv_field_3d
+        dd = torch.from_numpy(dens).cuda()
+        dh2 = torch.full_like(dd, 0.25)
+        dco = torch.full_like(dd, 1e-4)
+        for _ in range(2):
+            compute_fuv_field_3d(dd, g0, cell, dh2, dco, nside)
+        torch.cuda.synchronize()
+        out["rays"] = 12 * nside * nside
+    elif args.profile == "solve":
+        s.reset()
+        ok = s.run(max_iterations=4000, convergence_tol=args.tol, mixed=True,
+                   n_allow=max(8, int(1e-5 * n)), w_chem=args.w_chem)
+        h = s.convergence_history()
+        out.update({"converged": bool(ok), "outer_iterations": s.iterations,
+                    "ms": s.elapsed_ms(), "gpu_launches": s.launch_count(),
+                    "cell_solves_per_cell": float(h[:, 8].sum() / n)})
+    else:
+        s.run(max_iterations=13, convergence_tol=1e-300, mixed=True, n_allow=0,
+              w_chem=args.w_chem)
+        out["kernel_times_ms"] = kernel_times(s, reps=1)
+    s.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -601,17 +668,30 @@ def main():
                          "per-iteration sample")
     ap.add_argument("--plain-full", action="store_true", help="same as --plain full")
     ap.add_argument("--plain-iters", type=int, default=20)
-    ap.add_argument("--ref-iters", type=int, default=439,
+    ap.add_argument("--ref-iters", type=int, default=440,
                     help="outer iterations the reference arm is scaled by (the GPU solve of "
-                         "the 128^3 slab takes 439)")
+                         "the 128^3 slab takes 440)")
     ap.add_argument("--network-cells", type=int, default=1 << 20,
                     help="cells of the full-network measurement (0: skip)")
     ap.add_argument("--network-cpu-sample", type=int, default=2048)
     ap.add_argument("--production", type=int, default=1,
                     help="1: also solve the 256^3 production grid (one mixed solve) and "
                          "compare mixed with plain FP64 on a 64^3 subvolume")
+    ap.add_argument("--profile", default="", choices=["", "solve", "kernels", "rt"],
+                    help="a short run for ncu instead of the bench line: 'solve' = one mixed "
+                         "solve from the initial state (the launch list); 'kernels' = 13 mixed "
+                         "iterations, then one p3d_steady_kernel_times pass (the per-kernel "
+                         "counters: its mixed chemistry and thermal launches are the 14th of "
+                         "their kernels, the plain ones follow); 'rt' = two drop-in "
+                         "compute_fuv_field_3d calls after the solver's own ray march")
+    ap.add_argument("--launch", default="128,8",
+                    help="with --profile: per-cell launch shape (threads,blocks per SM) in "
+                         "place of the autotuner's choice")
     args = ap.parse_args()
     ws, rank, local = _dist()
+    if args.profile:
+        print(json.dumps(profile_run(args)))
+        return
     if ws > 1:
         import torch
         import torch.distributed as dist

@@ -382,6 +382,11 @@ int p3d_steady_adjoint(p3d_steady_t *s, const double *w6, double dx, int64_t max
  * iterations; the fastest is kept for later runs.  Resets the state before
  * returning.  cfg_out (optional): threads, blocks per SM; ms_out: its time. */
 int p3d_steady_autotune(p3d_steady_t *s, int warm_iters, int32_t *cfg_out, double *ms_out);
+/* Set the launch shape of the per-cell kernels directly (threads 128 or 256,
+ * 1-64 blocks per SM), e.g. one that p3d_steady_autotune chose earlier for
+ * the same grid.  The state is left as it is.  No counterpart in the
+ * reference. */
+int p3d_steady_set_launch(p3d_steady_t *s, int threads, int blocks_per_sm);
 /* Kernels launched on the device since the last p3d_steady_reset. */
 int p3d_steady_launch_count(p3d_steady_t *s, int64_t *out);
 /* Mean time (ms) over reps launches on the current state of: the three

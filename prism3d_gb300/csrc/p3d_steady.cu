@@ -366,21 +366,26 @@ int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, in
   if (stop > kMaxHist) return set_error(P3D_EINVAL, "iteration history full: reset first");
   bool done = false;
   cudaError_t e;
+  // one iteration: launch, synchronise, test
+  auto single = [&]() -> int {
+    int rc = launch_iteration(s, mixed != 0, par, str);
+    if (rc) return rc;
+    cudaError_t es = cudaMemcpyAsync(s->hist_host + kHistCols * it, s->hist + kHistCols * it,
+                                     sizeof(double) * kHistCols, cudaMemcpyDeviceToHost, str);
+    if (es == cudaSuccess) es = cudaStreamSynchronize(str);
+    if (es != cudaSuccess) return cuda_fail(es, "outer iteration");
+    s->launches += launches_per_iteration(s, mixed != 0);
+    s->last_dmax = s->hist_host[kHistCols * it];
+    bool c = conv(s->hist_host + kHistCols * it);
+    ++it;
+    if (c && it > 2) done = true;
+    return P3D_OK;
+  };
   if (!mixed || max_outer < kGraphIters) {
-    // plain path (and short mixed runs): launch, synchronise, test -- once
-    // per iteration
+    // plain path (and short mixed runs): once per iteration
     while (it < stop && !done) {
-      int rc = launch_iteration(s, mixed != 0, par, str);
+      int rc = single();
       if (rc) return rc;
-      e = cudaMemcpyAsync(s->hist_host + kHistCols * it, s->hist + kHistCols * it,
-                          sizeof(double) * kHistCols, cudaMemcpyDeviceToHost, str);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(str);
-      if (e != cudaSuccess) return cuda_fail(e, "plain iteration");
-      s->launches += launches_per_iteration(s, mixed != 0);
-      s->last_dmax = s->hist_host[kHistCols * it];
-      bool c = conv(s->hist_host + kHistCols * it);
-      ++it;
-      if (c && it > 2) done = true;
     }
   } else {
     // mixed path: a graph of kGraphIters iterations, tested per launch
@@ -402,7 +407,11 @@ int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, in
       s->graph_par = par;
     }
     while (it < stop && !done) {
-      if (it + kGraphIters > kMaxHist) return set_error(P3D_EINVAL, "iteration history full");
+      if (stop - it < kGraphIters) {  // the remainder, one at a time: max_outer is a cap
+        int rc = single();
+        if (rc) return rc;
+        continue;
+      }
       e = cudaGraphLaunch(s->graph, str);
       s->launches += (int64_t)launches_per_iteration(s, true) * kGraphIters;
       if (e == cudaSuccess)
@@ -751,6 +760,22 @@ int p3d_steady_autotune(p3d_steady_t* h, int warm_iters, int32_t* cfg_out, doubl
   if (cfg_out) { cfg_out[0] = bt; cfg_out[1] = bp; }
   if (ms_out) *ms_out = best;
   return p3d_steady_reset(h);
+}
+
+int p3d_steady_set_launch(p3d_steady_t* h, int threads, int blocks_per_sm) {
+  if (!h) return set_error(P3D_EINVAL, "null handle");
+  if (threads != 128 && threads != 256)
+    return set_error(P3D_EINVAL, "launch shape: threads %d not 128 or 256", threads);
+  if (blocks_per_sm < 1 || blocks_per_sm > 64)
+    return set_error(P3D_EINVAL, "launch shape: blocks per SM %d outside [1, 64]", blocks_per_sm);
+  SteadySolver* s = &h->s;
+  s->cell_threads = threads;
+  s->cell_per_sm = blocks_per_sm;
+  if (s->graph) {  // baked the old launch shape
+    cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+  }
+  return P3D_OK;
 }
 
 int p3d_steady_set_rate_scale(p3d_steady_t* h, const double* scale8) {

@@ -131,6 +131,12 @@ class PDRSolverGPU:
         self.iterations = 0
         return int(cfg[0]), int(cfg[1]), float(ms.value)
 
+    def set_launch(self, threads, blocks_per_sm):
+        """Set the per-cell kernels' launch shape directly (threads 128 or
+        256, 1-64 blocks per SM), e.g. one autotune() chose before for the
+        same grid; the state is kept."""
+        L.call("p3d_steady_set_launch", self._h, int(threads), int(blocks_per_sm))
+
     RATE_NAMES = ("H2_formation", "H2_photodiss", "H2_cr_destruction", "C_photoion",
                   "Cp_recombination", "CO_photodiss", "CO_cr_dissociation", "C_OH_to_CO")
 

@@ -95,6 +95,23 @@ def test_autotune_keeps_results():
     s.close()
 
 
+def test_max_iterations_is_a_cap():
+    """The mixed path runs graphs of eight iterations; a max_iterations that
+    is not a multiple of eight still stops there (the remainder one by one),
+    and graph and single launches give the same state."""
+    s, _ = _solver("cube16")
+    s.run(max_iterations=13, convergence_tol=1e-300, mixed=True, n_allow=0)
+    assert s.iterations == 13 and s.convergence_history().shape[0] == 13
+    ref = {k: s.get(k) for k in SPECIES + ("T_gas",)}
+    s.reset()
+    for _ in range(13):
+        s.run(max_iterations=1, convergence_tol=1e-300, mixed=True, n_allow=0)
+    assert s.iterations == 13
+    for k, v in ref.items():
+        np.testing.assert_array_equal(s.get(k), v)
+    s.close()
+
+
 def test_heating_cooling_diagnostics_and_saved_state(tmp_path):
     """Gamma and Lambda of the converged state (the reference stores them
     after each thermal solve, solver_3d.py:891-892) against the oracle's

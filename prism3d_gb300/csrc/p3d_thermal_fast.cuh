@@ -328,9 +328,11 @@ __device__ __forceinline__ double root_plain(const ThermalCtx& c, const LineFast
 // Finish: up to three FP64 Newton steps with the FP32 slope of T's
 // continuous piece (slope32; relative error ~1e-3), done once a step stays
 // in the bracket and moves T by at most 1e-8 T (the slope error then bounds
-// the remaining error by ~1e-11 T); else a two-point FP64 check for a jump
-// of the net heating at T, else the safeguarded FP64 iteration of
-// root_plain to tol.
+// the remaining error by ~1e-11 T); a step past an end of the bracket first
+// tests for a root within tol of that end (one FP64 evaluation at tol/2
+// inside it: a root there would otherwise be reached by bisection, ~20
+// evaluations); else a two-point FP64 check for a jump of the net heating at
+// T, else the safeguarded FP64 iteration of root_plain to tol.
 // A warm cell replays the last full bisection's decisions when its inputs
 // moved by less than margin / kReuseFactor (relative): the net heating's terms
 // then change by far less than the smallest certified |net| of those
@@ -451,7 +453,7 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LineFast
   double t, a = 0.0, b = 0.0, d_jump = 0.0, fa = 0.0, slope = 0.0, res = 0.0;
   double dx_old = 0.0, dx = 0.0;
   int ph, k = 0, st = 1;
-  bool at_lo = false;
+  bool at_lo = false, tried_lo = false, tried_hi = false;
   // (closed: a root returned on a discontinuity can be a bracket end, e.g.
   // 100 K, a node of the bisection tree)
   if (t_warm >= t_lo && t_warm <= t_hi) {
@@ -542,7 +544,7 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LineFast
       }
       case kNewton: {  // up to three FP64 Newton steps
         if (f > 0.0) t_lo = fmax(t_lo, t); else t_hi = fmin(t_hi, t);
-        if (f == 0.0) {
+        if (f == 0.0 || t_hi - t_lo <= tol * t) {  // (the latter: closed by an end check)
           st = 0;
           res = t;
           ph = kDone;
@@ -550,7 +552,20 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LineFast
         }
         const double tn = t - f / slope;
         if (!(slope < 0.0 && tn > t_lo && tn < t_hi)) {
-          ph = kJumpA;
+          // a step past an end of the bracket: the root may sit within tol of
+          // that end (10 K, a discontinuity at a node such as 100 K, or a
+          // node the outer iteration has pushed the cell's balance onto); one
+          // evaluation at tol/2 inside that end settles it, once per end
+          const double e_lo = t_lo * (1.0 + 0.5 * tol), e_hi = t_hi * (1.0 - 0.5 * tol);
+          if (slope < 0.0 && tn <= t_lo && !tried_lo && e_lo < t_hi) {
+            tried_lo = true;
+            t = e_lo;
+          } else if (slope < 0.0 && tn >= t_hi && !tried_hi && e_hi > t_lo) {
+            tried_hi = true;
+            t = e_hi;
+          } else {
+            ph = kJumpA;
+          }
         } else {
           const bool small = fabs(tn - t) <= fmax(1e-8, tol) * t;
           t = tn;
@@ -577,7 +592,17 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LineFast
           break;
         }
         double tn = t - f / slope;
-        if (!(slope < 0.0) || !(tn > t_lo && tn < t_hi) || fabs(2.0 * f) > fabs(dx_old * slope)) {
+        const double e_lo = t_lo * (1.0 + 0.5 * tol), e_hi = t_hi * (1.0 - 0.5 * tol);
+        if (slope < 0.0 && tn <= t_lo && !tried_lo && e_lo < t_hi) {  // end checks as above
+          tried_lo = true;
+          dx_old = dx;
+          tn = e_lo;
+        } else if (slope < 0.0 && tn >= t_hi && !tried_hi && e_hi > t_lo) {
+          tried_hi = true;
+          dx_old = dx;
+          tn = e_hi;
+        } else if (!(slope < 0.0) || !(tn > t_lo && tn < t_hi) ||
+                   fabs(2.0 * f) > fabs(dx_old * slope)) {
           dx_old = dx;
           tn = 0.5 * (t_lo + t_hi);
         } else {

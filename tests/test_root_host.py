@@ -87,6 +87,16 @@ def test_cold_mixed_root_matches_plain(lib, contexts):
     assert np.mean(rel <= 1e-6) >= 0.999, np.sort(rel)[-10:]
     # every full bisection left a node of the tree's last level
     assert np.all((node >= 1024) & (node < 2048))
+    # FP64 work: a root within tol of a bracket end (pinned at 10 K, or on
+    # the 100 K discontinuity, a node of the tree) costs two evaluations --
+    # the Newton step that leaves the bracket and the end check -- instead
+    # of a bisection creeping towards the end (~25)
+    pinned = tm <= 10.0 * (1.0 + TOL)
+    on_100 = np.abs(tm - 100.0) <= 100.0 * TOL
+    assert pinned.any() and on_100.any()
+    assert np.all(ev[pinned] <= 2), np.bincount(ev[pinned])
+    assert np.mean(ev[on_100] <= 2) >= 0.99, np.bincount(ev[on_100])
+    assert ev.mean() < 2.5, ev.mean()
 
 
 def test_warm_root_is_a_sign_change_and_pinned_roots_cost_one_evaluation(lib, contexts):
@@ -116,7 +126,40 @@ def test_warm_root_is_a_sign_change_and_pinned_roots_cost_one_evaluation(lib, co
     tc, evc, _ = _mixed(lib, c6, np.zeros(n), np.full(n, np.inf), nc, mc)
     rel = np.abs(tw - tc) / tc
     assert np.mean(rel <= 1e-6) >= 0.99, np.sort(rel)[-10:]
-    assert ev.mean() < evc.mean()
+    assert ev.mean() < 2.5 and ev.max() <= 32, (ev.mean(), ev.max())
+
+
+def test_root_at_a_bracket_end_costs_one_end_check(lib, contexts):
+    """A balance the outer iteration has pushed onto a node of the bisection
+    tree: the root sits within tol above the node, the bracket's lower end
+    (1000 K is the first decision).  Cells of this kind alternate between
+    branches from one outer iteration to the next and make the slow tail of
+    a solve; their Newton step from the bracket's middle lands just past the
+    end.  Built here from the oracle's contexts whose plain root lies in
+    [300, 3000] K by moving Gamma_fixed so that the root is 1000 (1 + 3e-11)
+    K: the mixed root lands within tol of it with at most three FP64
+    evaluations (the FP64 sign at the 1000 K node, the Newton step, the end
+    check) where the bisection towards the end took ~20, cold and warm from
+    the other branch (100 K) alike."""
+    ctx = contexts[1]
+    tp, _, _ = _plain(lib, ctx)
+    sel = np.where((tp > 300.0) & (tp < 3000.0))[0][:256]
+    assert sel.size >= 64
+    c = ctx[sel].copy()
+    t_root = 1000.0 * (1.0 + 3e-11)
+    c[:, 0] -= _net(lib, c, np.full(sel.size, t_root))
+    f_below = _net(lib, c, np.full(sel.size, 1000.0))
+    f_above = _net(lib, c, np.full(sel.size, 1000.0 * (1.0 + 1e-10)))
+    ok = (f_below > 0.0) & (f_above <= 0.0)  # the net heating falls through the root
+    assert ok.mean() > 0.9
+    c = np.ascontiguousarray(c[ok])
+    n = c.shape[0]
+    for t_warm in (np.zeros(n), np.full(n, 100.0)):
+        node, margin = np.zeros(n, np.int32), np.zeros(n, np.float32)
+        tm, ev, st = _mixed(lib, c, t_warm, np.full(n, np.inf), node, margin)
+        assert st.sum() == 0
+        assert np.all(np.abs(tm - t_root) <= TOL * t_root), np.abs(tm - t_root).max()
+        assert ev.max() <= 3, np.bincount(ev)
 
 
 def test_mixed_root_in_the_outer_loop_reaches_the_plain_fixed_point(lib, monkeypatch):

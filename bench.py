@@ -263,9 +263,8 @@ def run_gb300(args, ws, rank, local):
                      "unit": "TFLOP/s", "frac": cell_tf / fp64_peak,
                      "traffic": DRAM_BYTES_PER_CELL_SOLVE * n,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
-                                       "chemistry and thermal kernels on the 96^3 slab, every "
-                                       "cell solved, scaled by cells (bytes per launch pair, the "
-                                       "mark kernel not included)",
+                                       "chemistry and thermal launches of this pass at 128^3, "
+                                       "per cell solved, times n (the mark kernel not included)",
                      "peak_source": "measured live: DFMA-chain kernel on this GPU",
                      "algorithmic_flops_per_launch": FP64_OPS_PER_CELL_SOLVE * n,
                      "per_unit": f"{FP64_OPS_PER_CELL_SOLVE:.0f} FP64 flops per cell solve "
@@ -482,16 +481,17 @@ def network_bench(args):
 # on `bench.py --profile kernels` / `--profile rt` at 128^3 (2,097,152
 # cells; profiles/cell_kernels_slab128.md, profiles/columns_rt_slab128.md):
 # FP64 flops (DFMA = 2, DADD / DMUL = 1) per cell solve of the mixed
-# chemistry (1,827) and thermal (1,487) kernels on the 14th outer iteration,
-# every cell solved with exact roots, and their FP32 flops (757 + 5,960);
-# DRAM bytes of the two launches (read + write: 310.7 + 203.6 and 508.8 +
-# 173.8 MB): the state is streamed once per solve, so the traffic scales
+# chemistry (1,401) and thermal (1,246) kernels on the 14th outer iteration,
+# every cell solved with exact roots, and their FP32 flops (758 + 5,946);
+# DRAM bytes of the two launches (read + write: 310.6 + 203.6 and 509.4 +
+# 171.7 MB): the state is streamed once per solve, so the traffic scales
 # with the cells solved.
-FP64_OPS_PER_CELL_SOLVE = 1827.3 + 1487.3
-FP32_OPS_PER_CELL_SOLVE = 757.5 + 5960.1
-DRAM_BYTES_PER_CELL_SOLVE = (310.7 + 203.6 + 508.8 + 173.8) * 1e6 / 2097152
-FP64_PIPE_ACTIVE_NCU = ("86% (chemistry), 79% (thermal): the pipe also runs FP64 compares, "
-                        "min/max and FP32<->FP64 conversions")
+FP64_OPS_PER_CELL_SOLVE = 1401.4 + 1245.6
+FP32_OPS_PER_CELL_SOLVE = 757.5 + 5945.7
+DRAM_BYTES_PER_CELL_SOLVE = (310.6 + 203.6 + 509.4 + 171.7) * 1e6 / 2097152
+FP64_PIPE_ACTIVE_NCU = ("86% (chemistry), 62% (thermal): the pipe also runs FP64 compares, "
+                        "min/max and FP32<->FP64 conversions; the thermal kernel's remaining "
+                        "time is latency of divergent root paths")
 # columns launch: FP64-pipe bound (82% busy), 27 FP64 flops per cell; DRAM
 # per launch (read + write) with the chemistry's layers partly L2-resident
 COLUMNS_DRAM_BYTES_PER_CELL = (55.9 + 6.0) * 1e6 / 2097152

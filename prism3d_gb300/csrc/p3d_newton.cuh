@@ -41,12 +41,14 @@ struct ChemCell {
 
 // Shielding factors and the photo rates they set, once per cell when the
 // columns are fixed for the whole solve.
+// FAST: the mixed path's form of the CO shielding (fsh_co).
+template <bool FAST = false>
 __device__ __forceinline__ void chem_prepare(ChemCell& p) {
   if (p.ds > 0.0) return;
   double d1, dh;
   p.fh2_fix = fsh_h2(p.u_h2, p.b_dop, &d1);
   p.kpd_fix = p.kpd0 * p.fh2_fix;
-  p.kco_fix = p.kco0 * fsh_co(p.u_co, p.u_h2, &dh) + p.kco_cr;
+  p.kco_fix = p.kco0 * fsh_co<FAST>(p.u_co, p.u_h2, &dh) + p.kco_cr;
 }
 
 __device__ __forceinline__ void chem5_eval(const ChemCell& p, const double* y, double* f,

@@ -2,6 +2,7 @@
 #pragma once
 
 #include "p3d_common.cuh"
+#include "p3d_fastexp.cuh"
 
 namespace p3d {
 
@@ -32,15 +33,34 @@ __device__ __forceinline__ double fsh_h2_dlnb(double n, double b, double f) {
   return 2.0 * 0.965 * xb / (q * q * q * fmax(f, 1e-300));
 }
 
-// f_shield_CO (shielding.py:136-171) and its N_H2 derivative.
+// f_shield_CO (shielding.py:136-171) and its N_H2 derivative.  FAST (the
+// mixed-precision path): the four power laws come from two logarithms (x^a =
+// exp(a ln x)) and the exponentials from exp64, with exp(-A) exp(-B) =
+// exp(-(A + B)) -- on GB300 the FP64 operations of four pow() calls are a
+// large part of the chemistry kernel, which evaluates this once per cell and
+// outer iteration; relative difference from the pow() form <= ~1e-13 (the
+// error of ln x times a ln x <= ~25 for the columns met).  The plain FP64
+// path keeps the pow() form.
+template <bool FAST = false>
 __device__ __forceinline__ double fsh_co(double nco_in, double nh2_in, double* d_h2) {
   double nco = fmax(nco_in, 1.0), nh2 = fmax(nh2_in, 1.0);
-  double A = 6.428e-8 * pow(nco, 0.53);
-  double B = 3.0e-12 * pow(nh2, 0.495);
-  double Cc = 1e-5 * pow(nco, 0.6);
-  double P4 = pow(nh2, 0.48);
-  double E = exp(-8e-12 * P4);
-  double f = exp(-A) * exp(-B) * (1.0 / (1.0 + Cc * E));
+  double A, B, Cc, P4, E, f;
+  if (FAST) {
+    const double lco = log(nco), lh2 = log(nh2);
+    A = 6.428e-8 * exp64(0.53 * lco);
+    B = 3.0e-12 * exp64(0.495 * lh2);
+    Cc = 1e-5 * exp64(0.6 * lco);
+    P4 = exp64(0.48 * lh2);
+    E = exp64(-8e-12 * P4);
+    f = exp64(-(A + B)) * (1.0 / (1.0 + Cc * E));
+  } else {
+    A = 6.428e-8 * pow(nco, 0.53);
+    B = 3.0e-12 * pow(nh2, 0.495);
+    Cc = 1e-5 * pow(nco, 0.6);
+    P4 = pow(nh2, 0.48);
+    E = exp(-8e-12 * P4);
+    f = exp(-A) * exp(-B) * (1.0 / (1.0 + Cc * E));
+  }
   bool live = (f > 1e-10 && f < 1.0);
   *d_h2 = (live && nh2_in > 1.0)
               ? f * (-0.495 * B / nh2 + Cc * E * 8e-12 * 0.48 * P4 / (nh2 * (1.0 + Cc * E)))

@@ -558,7 +558,9 @@ ss_chem_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g,
     ChemCell cc;
     cc.n_h = nh;
     cc.kci = d.kci[i] * p.rs[3];
-    cc.acp = 4.67e-12 * pow(tg / 300.0, -0.6) * p.rs[4];
+    // (T / 300)^-0.6; the mixed path from a logarithm and exp64 (as fsh_co)
+    cc.acp = 4.67e-12 * (MIXED ? exp64(-0.6 * log(tg / 300.0)) : pow(tg / 300.0, -0.6)) *
+             p.rs[4];
     cc.rh2 = rh2 * nh * 0.5 * p.rs[0];
     cc.rcr = 2.5 * zeta * 0.1 * p.rs[2];
     cc.xc = p.x_c_total;
@@ -571,7 +573,7 @@ ss_chem_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g,
     cc.u_co = d.u_co[i];
     cc.ds = p.h2_implicit ? d.ds[i] : 0.0;
     cc.b_dop = b_dop;
-    chem_prepare(cc);
+    chem_prepare<MIXED>(cc);
     double y[5];
 #pragma unroll
     for (int c = 0; c < 5; ++c) y[c] = fmax(y_old[c], 1e-30);

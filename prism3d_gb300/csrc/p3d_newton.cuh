@@ -283,9 +283,11 @@ __device__ __forceinline__ int chem_steady_cell(const ChemCell& p, double* y, in
     }
     inv_dt /= growth;
   }
-  {  // f_H2 at the final state
+  if (p.ds > 0.0) {  // f_H2 at the final state (fixed by the columns otherwise)
     double f[5], J[5][5], sc[5];
     chem5_eval(p, y, f, J, sc, fh2);
+  } else {
+    *fh2 = p.fh2_fix;
   }
   *iters = it;
   return status;

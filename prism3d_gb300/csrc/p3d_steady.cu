@@ -357,7 +357,7 @@ int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, in
   par.quiet_in_tol = tol;
   // the Doppler width reaches a cell only through f_H2: held to the columns'
   // tolerance
-  par.quiet_b_tol = tol * 0.1;
+  par.quiet_b_tol = tol;
   // a small step alone does not make a cell settled: a T update confined to
   // a stale bracket (or hopping across a collapsed one) moves T by ~1e-12
   // while G(T) - T stays large, and only re-solving the cell breaks such a

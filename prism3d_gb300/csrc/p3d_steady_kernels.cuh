@@ -536,7 +536,9 @@ ss_chem_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g,
   const int64_t count = MIXED ? (int64_t)g->n_active : n;
   unsigned int my_fail = 0u;
   const int lane = threadIdx.x & 31;
-  for (;;) {  // 32 cells per warp from a global counter (as the thermal kernel)
+  // warps past the list's batches of 32 take none (as the thermal kernel)
+  const bool queue = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) < (count + 31) / 32;
+  while (queue) {  // 32 cells per warp from a global counter (as the thermal kernel)
     unsigned int base = 0u;
     if (lane == 0) base = atomicAdd(&g->chem_next, 32u);
     base = __shfl_sync(0xffffffffu, base, 0);
@@ -679,9 +681,13 @@ ss_thermal_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
   unsigned long long my_evals = 0ull;
   // Warps take 32 cells (mixed: list entries) at a time from a global
   // counter, so the uneven root-finding work spreads over all warps until
-  // none is left.
+  // none is left.  Warps past the list's batches of 32 take none: in the
+  // last outer iterations a few thousand listed cells meet a grid sized for
+  // every cell, and each idle warp's queue atomic would queue up on the
+  // counter.
   const int lane = threadIdx.x & 31;
-  for (;;) {
+  const bool queue = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) < (count + 31) / 32;
+  while (queue) {
     unsigned int base = 0u;
     if (lane == 0) base = atomicAdd(&g->therm_next, 32u);
     base = __shfl_sync(0xffffffffu, base, 0);
@@ -751,7 +757,7 @@ ss_thermal_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
     for (int k = 0; k < 3; ++k) my_gt[k] += __shfl_xor_sync(0xffffffffu, my_gt[k], o);
   }
   if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&g->evals64, my_evals);
+    if (my_evals) atomicAdd(&g->evals64, my_evals);
     if (my_fail) atomicAdd(&g->therm_fail, my_fail);
 #pragma unroll
     for (int k = 0; k < 3; ++k)

@@ -481,15 +481,15 @@ def network_bench(args):
 # on `bench.py --profile kernels` / `--profile rt` at 128^3 (2,097,152
 # cells; profiles/cell_kernels_slab128.md, profiles/columns_rt_slab128.md):
 # FP64 flops (DFMA = 2, DADD / DMUL = 1) per cell solve of the mixed
-# chemistry (1,401) and thermal (1,246) kernels on the 14th outer iteration,
+# chemistry (1,403) and thermal (1,243) kernels on the 14th outer iteration,
 # every cell solved with exact roots, and their FP32 flops (758 + 5,946);
-# DRAM bytes of the two launches (read + write: 310.6 + 203.6 and 509.4 +
-# 171.7 MB): the state is streamed once per solve, so the traffic scales
+# DRAM bytes of the two launches (read + write: 327.4 + 204.8 and 530.3 +
+# 260.7 MB): the state is streamed once per solve, so the traffic scales
 # with the cells solved.
-FP64_OPS_PER_CELL_SOLVE = 1401.4 + 1245.6
+FP64_OPS_PER_CELL_SOLVE = 1402.7 + 1242.9
 FP32_OPS_PER_CELL_SOLVE = 757.5 + 5945.7
-DRAM_BYTES_PER_CELL_SOLVE = (310.6 + 203.6 + 509.4 + 171.7) * 1e6 / 2097152
-FP64_PIPE_ACTIVE_NCU = ("86% (chemistry), 62% (thermal): the pipe also runs FP64 compares, "
+DRAM_BYTES_PER_CELL_SOLVE = (327.4 + 204.8 + 530.3 + 260.7) * 1e6 / 2097152
+FP64_PIPE_ACTIVE_NCU = ("86% (chemistry), 70% (thermal): the pipe also runs FP64 compares, "
                         "min/max and FP32<->FP64 conversions; the thermal kernel's remaining "
                         "time is latency of divergent root paths")
 # columns launch: FP64-pipe bound (82% busy), 27 FP64 flops per cell; DRAM

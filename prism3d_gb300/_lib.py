@@ -68,6 +68,7 @@ SIGNATURES = {
     "p3d_steady_set_rate_scale": [_vp, _D],
     "p3d_steady_autotune": [_vp, ctypes.c_int, _I32, _D],
     "p3d_steady_set_launch": [_vp, ctypes.c_int, ctypes.c_int],
+    "p3d_steady_set_coop_max": [_vp, _i64],
     "p3d_steady_set_fixed_temperature": [_vp, ctypes.c_int],
     "p3d_steady_adjoint": [_vp, _D, _f64, _i64, _f64, _f64, _D, _D, _D, _I64, _I64],
     "p3d_network_create": [ctypes.POINTER(_vp), _i32, _i32, _I32, _D, _D, _D, _I32, _I32, _I32,

@@ -183,6 +183,9 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   for (int k = 0; k < 8; ++k) p.rs[k] = 1.0;
   p.fix_t = 0;
   p.exact_roots = 0;
+  // one cell per warp below ~2 cells per FP64 unit (608 schedulers): above
+  // that, 32 cells per warp keep more of the units busy
+  p.coop_max = 2048;
   p.quiet_tol = p.quiet_in_tol = p.quiet_b_tol = p.quiet_r_tol = 0.0;
   p.pe = PeGrid{log_psi_min, log_psi_step, eg_min, eg_step, (int)n_psi, (int)n_eg};
   memcpy(p.lines.cii, cii, sizeof(p.lines.cii));
@@ -274,6 +277,7 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
                            s->a_nano, s->a_rest, str);
   if (e == cudaSuccess) {
     ss_bisect_table_kernel<<<1, 32, 0, str>>>();
+    ss_coop_table_kernel<<<1, 64, 0, str>>>(p.lf);
     e = cudaGetLastError();
   }
   {
@@ -779,6 +783,17 @@ int p3d_steady_set_launch(p3d_steady_t* h, int threads, int blocks_per_sm) {
   if (s->graph) {  // baked the old launch shape
     cudaGraphExecDestroy(s->graph);
     s->graph = nullptr;
+  }
+  return P3D_OK;
+}
+
+int p3d_steady_set_coop_max(p3d_steady_t* h, int64_t max_cells) {
+  if (!h) return set_error(P3D_EINVAL, "null handle");
+  if (max_cells < 0) return set_error(P3D_EINVAL, "coop_max must be >= 0");
+  h->s.par.coop_max = (int)(max_cells > INT32_MAX ? INT32_MAX : max_cells);
+  if (h->s.graph) {  // baked the old parameters
+    cudaGraphExecDestroy(h->s.graph);
+    h->s.graph = nullptr;
   }
   return P3D_OK;
 }

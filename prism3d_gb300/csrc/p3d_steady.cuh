@@ -66,6 +66,9 @@ struct SteadyParams {
   double rs[8];
   int fix_t;  // 1: T_gas is held at its current value (no thermal balance)
   int exact_roots;  // 1: mixed thermal roots to therm_tol_mixed even while a cell moves
+  // mixed thermal kernel: lists of at most this many cells are solved one
+  // cell per warp, the FP64 net heating evaluated by the whole warp
+  int coop_max;
   PeGrid pe;
   LineParams lines;
   LineFast lf;  // make_line_fast(lines)

@@ -41,6 +41,14 @@ __device__ double g_bisect_mid[1024];
 // per node: the FP32 twin's temperature-only FP64 parts (p3d_thermal_fast.cuh)
 __device__ BisectNode g_bisect_node[1024];
 
+// the two-level line table of the warp-cooperative net heating
+__device__ CoopLine g_coop_lines[kCoopLines];
+
+__global__ void ss_coop_table_kernel(LineFast lf) {
+  const int e = threadIdx.x;
+  if (blockIdx.x == 0 && e < kCoopLines) g_coop_lines[e] = coop_line(e, lf, c_co_ss);
+}
+
 __global__ void ss_bisect_table_kernel() {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double lo[1024], hi[1024];
@@ -664,8 +672,73 @@ ss_heating_cooling_kernel(int64_t n, SteadyDev d, SteadyParams p, int which,
   }
 }
 
-// Thermal context (solver_3d.py:693-754), thermal root, per-cell T update,
-// convergence measure.
+// Thermal context (solver_3d.py:693-754), thermal root, per-cell T update and
+// convergence measure of cell i.  COOP: all lanes of the warp run it for the
+// same cell (FP64 net heating over the warp); only `lead` stores and counts.
+template <bool MIXED, bool COOP>
+__device__ __forceinline__ void thermal_cell(int64_t i, const SteadyDev& d, const SteadyParams& p,
+                                             double b_dop, bool lead, double& my_max,
+                                             unsigned int* my_gt, unsigned int& my_fail,
+                                             unsigned long long& my_evals) {
+  const double tg = d.t_gas[i];
+  const ThermalCtx c = steady_thermal_ctx(d, i);
+  int tst = 0, nev = 0;
+  double troot;
+  int node = 0;
+  float margin = 0.0f;
+  if (p.fix_t) {
+    troot = tg;
+  } else if (MIXED) {
+    // largest relative change of the root's inputs since the cell's last
+    // thermal solve: species, T (context), H2/CO columns, Doppler width
+    const double tp0 = d.t_prev[i];
+    double delta = fmax(d.chg_spec[i], tp0 > 0.0 ? fabs(tg - tp0) / tg : INFINITY);
+    delta = fmax(delta, fabs(d.u_h2[i] - d.u_h2_last[i]) / fmax(fabs(d.u_h2[i]), 1e-300));
+    delta = fmax(delta, fabs(d.u_co[i] - d.u_co_last[i]) / fmax(fabs(d.u_co[i]), 1e-300));
+    delta = fmax(delta, fabs(b_dop - d.b_last[i]) / b_dop);
+    node = d.bis_node[i];
+    margin = d.bis_margin[i];
+    // inexact roots while the cell is still moving: the root tolerance
+    // follows 1% of its last relative change (at most 1e-4), back to
+    // therm_tol_mixed as it settles; a cell's first solve is exact
+    const double cl = d.chg_last[i];
+    const double rtol_t = (isfinite(cl) && !p.exact_roots)
+                              ? fmax(p.therm_tol_mixed, fmin(1e-4, 0.01 * cl))
+                              : p.therm_tol_mixed;
+    troot = root_mixed<COOP>(c, p.lf, c_co_ss, p.theta2, c_lines32, c_co32, g_bisect_mid,
+                             g_bisect_node, rtol_t, p.therm_max_iter, d.t_root[i], delta, &node,
+                             &margin, &tst, &nev, g_coop_lines);
+  } else {
+    troot = root_plain(c, p.lf, c_co_ss, p.theta2, p.therm_tol, p.therm_max_iter, &tst, &nev);
+  }
+  double tp = d.t_prev[i], rp = d.r_prev[i], lo = d.t_lo[i], hi = d.t_hi[i], sp = d.span[i];
+  double tn = t_update(tg, troot, p.w_t, tp, rp, lo, hi, sp);
+  double m = fmax(d.chg_spec[i], fabs(tn - tg) / tg);
+  if (!(m == m)) m = INFINITY;
+  if (!lead) return;
+  if (MIXED && !p.fix_t) {
+    d.bis_node[i] = (int16_t)node;
+    d.bis_margin[i] = margin;
+  }
+  my_evals += (unsigned long long)nev;
+  my_fail += (unsigned)tst;
+  my_max = fmax(my_max, m);
+  my_gt[0] += m > p.count_thr[0];
+  my_gt[1] += m > p.count_thr[1];
+  my_gt[2] += m > p.count_thr[2];
+  d.t_root[i] = troot;
+  d.t_gas[i] = tn;
+  d.t_prev[i] = tp;
+  d.r_prev[i] = rp;
+  d.t_lo[i] = lo;
+  d.t_hi[i] = hi;
+  d.span[i] = sp;
+  d.u_h2_last[i] = d.u_h2[i];
+  d.u_co_last[i] = d.u_co[i];
+  d.b_last[i] = b_dop;
+  d.chg_last[i] = m;
+}
+
 // __maxnreg__ 80 (6 resident blocks of 128 threads per SM instead of 4 at
 // the 124 registers the compiler picks): the thermal launches of the tail are
 // latency-bound and gain from more warps despite a few spills (a 1.9% shorter
@@ -679,75 +752,41 @@ ss_thermal_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
   unsigned int my_gt[3] = {0u, 0u, 0u};
   unsigned int my_fail = 0u;
   unsigned long long my_evals = 0ull;
-  // Warps take 32 cells (mixed: list entries) at a time from a global
-  // counter, so the uneven root-finding work spreads over all warps until
-  // none is left.  Warps past the list's batches of 32 take none: in the
-  // last outer iterations a few thousand listed cells meet a grid sized for
-  // every cell, and each idle warp's queue atomic would queue up on the
-  // counter.
   const int lane = threadIdx.x & 31;
-  const bool queue = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) < (count + 31) / 32;
-  while (queue) {
-    unsigned int base = 0u;
-    if (lane == 0) base = atomicAdd(&g->therm_next, 32u);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if ((int64_t)base >= count) break;
-    const int64_t k = (int64_t)base + lane;
-    if (k >= count) continue;
-    const int64_t i = MIXED ? (int64_t)d.list[k] : k;
-    const double tg = d.t_gas[i];
-    const ThermalCtx c = steady_thermal_ctx(d, i);
-    int tst = 0, nev = 0;
-    double troot;
-    if (p.fix_t) {
-      troot = tg;
-    } else if (MIXED) {
-      // largest relative change of the root's inputs since the cell's last
-      // thermal solve: species, T (context), H2/CO columns, Doppler width
-      const double tp0 = d.t_prev[i];
-      double delta = fmax(d.chg_spec[i], tp0 > 0.0 ? fabs(tg - tp0) / tg : INFINITY);
-      delta = fmax(delta, fabs(d.u_h2[i] - d.u_h2_last[i]) / fmax(fabs(d.u_h2[i]), 1e-300));
-      delta = fmax(delta, fabs(d.u_co[i] - d.u_co_last[i]) / fmax(fabs(d.u_co[i]), 1e-300));
-      delta = fmax(delta, fabs(b_dop - d.b_last[i]) / b_dop);
-      int node = d.bis_node[i];
-      float margin = d.bis_margin[i];
-      // inexact roots while the cell is still moving: the root tolerance
-      // follows 1% of its last relative change (at most 1e-4), back to
-      // therm_tol_mixed as it settles; a cell's first solve is exact
-      const double cl = d.chg_last[i];
-      const double rtol_t = (isfinite(cl) && !p.exact_roots)
-                                ? fmax(p.therm_tol_mixed, fmin(1e-4, 0.01 * cl))
-                                : p.therm_tol_mixed;
-      troot = root_mixed(c, p.lf, c_co_ss, p.theta2, c_lines32, c_co32, g_bisect_mid, g_bisect_node,
-                         rtol_t, p.therm_max_iter, d.t_root[i], delta, &node, &margin, &tst,
-                         &nev);
-      d.bis_node[i] = (int16_t)node;
-      d.bis_margin[i] = margin;
-    } else {
-      troot = root_plain(c, p.lf, c_co_ss, p.theta2, p.therm_tol, p.therm_max_iter, &tst,
-                         &nev);
+  const int64_t gwarp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (MIXED && count <= (int64_t)p.coop_max) {
+    // a short list (the last outer iterations): one cell per warp.  The
+    // launch then lasts as long as the slowest cell's chain of FP64
+    // evaluations, and on GB300 a warp's FP64 instruction holds its
+    // scheduler's FP64 unit as long with one active lane as with 32: the
+    // warp evaluates the cell's net heating together (net_heating_coop64).
+    bool queue = gwarp < count;
+    while (queue) {
+      unsigned int base = 0u;
+      if (lane == 0) base = atomicAdd(&g->therm_next, 1u);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if ((int64_t)base >= count) break;
+      thermal_cell<MIXED, true>((int64_t)d.list[base], d, p, b_dop, lane == 0, my_max, my_gt,
+                                my_fail, my_evals);
     }
-    my_evals += (unsigned long long)nev;
-    my_fail += (unsigned)tst;
-    double tp = d.t_prev[i], rp = d.r_prev[i], lo = d.t_lo[i], hi = d.t_hi[i], sp = d.span[i];
-    double tn = t_update(tg, troot, p.w_t, tp, rp, lo, hi, sp);
-    double m = fmax(d.chg_spec[i], fabs(tn - tg) / tg);
-    if (!(m == m)) m = INFINITY;
-    my_max = fmax(my_max, m);
-    my_gt[0] += m > p.count_thr[0];
-    my_gt[1] += m > p.count_thr[1];
-    my_gt[2] += m > p.count_thr[2];
-    d.t_root[i] = troot;
-    d.t_gas[i] = tn;
-    d.t_prev[i] = tp;
-    d.r_prev[i] = rp;
-    d.t_lo[i] = lo;
-    d.t_hi[i] = hi;
-    d.span[i] = sp;
-    d.u_h2_last[i] = d.u_h2[i];
-    d.u_co_last[i] = d.u_co[i];
-    d.b_last[i] = b_dop;
-    d.chg_last[i] = m;
+  } else {
+    // Warps take 32 cells (mixed: list entries) at a time from a global
+    // counter, so the uneven root-finding work spreads over all warps until
+    // none is left.  Warps past the list's batches of 32 take none: in the
+    // last outer iterations a few thousand listed cells meet a grid sized
+    // for every cell, and each idle warp's queue atomic would queue up on
+    // the counter.
+    const bool queue = gwarp < (count + 31) / 32;
+    while (queue) {
+      unsigned int base = 0u;
+      if (lane == 0) base = atomicAdd(&g->therm_next, 32u);
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if ((int64_t)base >= count) break;
+      const int64_t k = (int64_t)base + lane;
+      if (k >= count) continue;
+      thermal_cell<MIXED, false>(MIXED ? (int64_t)d.list[k] : k, d, p, b_dop, true, my_max, my_gt,
+                                 my_fail, my_evals);
+    }
   }
   block_max_atomic(my_max, &g->dmax_bits);
   for (int o = 16; o > 0; o >>= 1) {

@@ -126,6 +126,125 @@ __device__ __noinline__ double net_heating_fast64(double t, const ThermalCtx& c,
   return net_heating_fast64_body(t, c, lf, co, theta2);
 }
 
+// ------------------------------------------- warp-cooperative FP64 net heating
+// The five fine-structure lines and the 40 CO levels as one table of
+// two-level lines, so that 32 lanes can evaluate one cell's lines with the
+// same instructions (entry e on lane e % 32):
+//   q = c1 T^a1 n_HI + c2 T^a2 n_H2 + c3 T^a3 exp(d3 / T) n_e,
+//   r = g q exp(-t_ul / T),   term = n_x r / (r + a + q) e,
+// n_x = n_C+ / n_H (0), n_O / n_H (1), n_C / n_H (2), n_CO (3).  Entries 0-4:
+// [CII] 158, [OI] 63, [OI] 145, [CI] 609, [CI] 370 (their collision rates as
+// in net_heating_fast64_body, the (T / 100)^a factors folded into c); 5-44:
+// CO levels J = 1-40 (q = 3.3e-12 (1 + 0.1 J) T^0.5 n_H2; active below the
+// ladder's break).
+struct CoopLine {
+  double c1, a1, c2, a2, c3, a3, d3, g, t_ul, a, e;
+  int species;
+};
+constexpr int kCoopLines = 45;
+
+__host__ __device__ inline CoopLine coop_line(int e, const LineFast& lf, const CoLevel* co) {
+  CoopLine L{};
+  const double l100 = 4.605170185988091368;  // ln 100
+  if (e >= 5) {
+    const CoLevel& v = co[e - 5];
+    L.c2 = 3.3e-12 * v.j_factor;
+    L.a2 = 0.5;
+    L.g = v.g_ratio;
+    L.t_ul = v.t_u;
+    L.a = v.a_co;
+    L.e = v.ahv;
+    L.species = 3;
+    return L;
+  }
+  L.g = lf.g_ratio[e];
+  L.t_ul = lf.t_ul[e];
+  L.a = lf.a[e];
+  L.e = lf.e[e];
+  if (e == 0) {
+    L.c1 = 8.0e-10 * exp(-0.07 * l100); L.a1 = 0.07;
+    L.c2 = 4.9e-10 * exp(-0.12 * l100); L.a2 = 0.12;
+    L.c3 = lf.cii_ce; L.a3 = -0.5; L.d3 = -lf.t_ul[0];
+    L.species = 0;
+  } else if (e <= 2) {
+    L.c1 = e == 1 ? 9.2e-12 : 4.0e-12; L.a1 = e == 1 ? 0.67 : 0.60;
+    L.c2 = e == 1 ? 4.5e-12 : 2.0e-12; L.a2 = e == 1 ? 0.64 : 0.58;
+    L.c3 = (e == 1 ? 1.4e-8 : 5.0e-9) * exp(-0.39 * l100); L.a3 = 0.39;
+    L.species = 1;
+  } else {
+    L.c1 = 1.0e-10 * exp(-0.3 * l100); L.a1 = 0.3;
+    L.c2 = 5.0e-11 * exp(-0.3 * l100); L.a2 = 0.3;
+    L.c3 = 2.0e-6; L.a3 = -0.5;
+    L.species = 2;
+  }
+  return L;
+}
+
+#ifdef __CUDA_ARCH__
+// The FP64 net heating of one cell at t, evaluated by all 32 lanes of a
+// warp together and returned to every lane: each lane takes the table
+// entries lane and lane + 32 (the CO Boltzmann factors from exp64 directly
+// rather than by recurrence), the remaining terms are computed on every
+// lane, the line terms are summed by a butterfly and lane 0's sum is
+// broadcast, so that every lane holds the same value.  Same terms as
+// net_heating_fast64_body; the summation order differs (relative difference
+// ~1e-15 of the terms).  On GB300 a warp's FP64 instruction holds its
+// scheduler's FP64 unit as long with one active lane as with 32, so a
+// warp evaluating one cell this way finishes ~5x sooner than a lane
+// evaluating it alone: the thermal kernel uses it when the list is short.
+__device__ __noinline__ double net_heating_coop64(double t, const ThermalCtx& c,
+                                                  const CoopLine* __restrict__ tab,
+                                                  const CoLevel* __restrict__ co,
+                                                  double theta2) {
+  const int lane = threadIdx.x & 31;
+  const double lt = log(t);
+  const double sqrt_t = sqrt(t);
+  const double inv_t = 1.0 / t;
+  const double inv_sqrt_t = sqrt_t * inv_t;
+  const int nlev = co_levels_below(5.0 * t, co);
+  double part = 0.0;
+  for (int e = lane; e < kCoopLines; e += 32) {
+    if (e >= 5 && e - 5 >= nlev) continue;
+    const CoopLine L = tab[e];
+    double q = L.c2 * exp64(L.a2 * lt) * c.n_h2;
+    if (L.c1 != 0.0) {
+      q += L.c1 * exp64(L.a1 * lt) * c.n_hi;
+      q += L.c3 * exp64(fma(L.d3, inv_t, L.a3 * lt)) * c.n_e;
+    }
+    const double r = L.g * q * exp64(-L.t_ul * inv_t);
+    const double nx = L.species == 3 ? c.n_co
+                      : (L.species == 0 ? c.n_cp_nh : (L.species == 1 ? c.n_o_nh : c.n_c_nh));
+    part += nx * (r / (r + L.a + q)) * L.e;
+  }
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  part = __shfl_sync(0xffffffffu, part, 0);
+  double net = c.gamma_fixed + c.gg_coeff * sqrt_t * (c.t_dust - t) - part;
+  if (t >= 100.0) {
+    double x = fmin(fmax(lt / kLn10, 2.0), 4.5);
+    double llh = -24.311 + x * (3.5692 + x * (-11.332 + x * (15.738 + x * (-10.581 +
+                 x * (3.5803 + x * -0.48365)))));
+    double llh2 = -24.311 + x * (4.6585 + x * (-14.272 + x * (19.779 + x * (-13.255 +
+                  x * (4.4840 + x * -0.60504)))));
+    double l0 = exp64(llh * kLn10) * c.n_hi + exp64(llh2 * kLn10) * c.n_h2;
+    double lte = exp64((-19.703 + 0.5 * x) * kLn10);
+    net -= c.n_h2 * l0 * lte / fmax(l0 + lte, 1e-50);
+  }
+  if (t >= 3000.0) net -= c.n_hi * c.n_e * (2.41e-6 * inv_sqrt_t * 0.486 * exp64(-1.18e5 * inv_t)) *
+                          10.2 * kEVtoErg;
+  {
+    double gg_cool = c.gg_coeff * sqrt_t * (t - c.t_dust);
+    if (gg_cool > 0.0) net -= gg_cool;
+  }
+  net -= c.n_cp_nh * c.n_e * (4.67e-12 * exp64(-0.6 * (lt - kLn300))) * kKBoltz * t;
+  (void)theta2;
+  return net;
+}
+#else
+// host builds (the CPU tests) have no warps: the lane-wise form
+inline double net_heating_coop64(double t, const ThermalCtx& c, const CoopLine*,
+                                 const CoLevel* co, double theta2);
+#endif
+
 // Per-cell FP32 coefficients, scaled by 1 / Gamma_fixed.
 struct ThermalCtx32 {
   float gg, td, ne, nhi, nh2, cii, o63, o145, ci609, ci370, co, h2, lya, rec;
@@ -389,6 +508,10 @@ __device__ __forceinline__ double slope32(double t, const ThermalCtx32& f32,
   return (double)(f0 - net_heating32(t - h, f32, lines32, co32, co, &S2)) / h;
 }
 
+// COOP: every lane of the warp runs this for the same cell (the control flow
+// is then uniform) and each FP64 evaluation is net_heating_coop64 over the
+// warp, with the table `coop`.
+template <bool COOP = false>
 __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LineFast& lf,
                                              const CoLevel* __restrict__ co, double theta2,
                                              const float* __restrict__ lines32,
@@ -397,7 +520,11 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LineFast
                                              const BisectNode* __restrict__ node_tab, double tol,
                                              int max_it, double t_warm, double delta,
                                              int* node_io, float* margin_io, int* status,
-                                             int* n64) {
+                                             int* n64, const CoopLine* coop = nullptr) {
+  auto eval64 = [&](double x) -> double {
+    if constexpr (COOP) return net_heating_coop64(x, c, coop, co, theta2);
+    else return net_heating_fast64(x, c, lf, co, theta2);
+  };
   double K;
   const ThermalCtx32 f32 = make_ctx32(c, lf, co, &K);
   double t_lo = 10.0, t_hi = 1e5;
@@ -423,7 +550,7 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LineFast
         pos = v > 0.0f;
         margin = fminf(margin, fabsf(v) / S);
       } else {
-        const double f = net_heating_fast64(t_mid, c, lf, co, theta2);
+        const double f = eval64(t_mid);
         pos = f > 0.0;
         ++evals;
         margin = fminf(margin, S > 0.0f ? (float)(fabs(f) / (double)S) : 0.0f);
@@ -499,7 +626,7 @@ __device__ __forceinline__ double root_mixed(const ThermalCtx& c, const LineFast
       ph = kNewton;
     }
     const double x = (ph == kNearA || ph == kJumpA) ? a : (ph == kNearB || ph == kJumpB) ? b : t;
-    const double f = net_heating_fast64(x, c, lf, co, theta2);
+    const double f = eval64(x);
     ++evals;
     switch (ph) {
       case kPinned:

@@ -137,6 +137,12 @@ class PDRSolverGPU:
         same grid; the state is kept."""
         L.call("p3d_steady_set_launch", self._h, int(threads), int(blocks_per_sm))
 
+    def set_coop_max(self, max_cells):
+        """Worklists of at most max_cells cells are solved one cell per warp
+        by the mixed thermal kernel (its FP64 net heating evaluated by the
+        whole warp; default 2048, 0 never)."""
+        L.call("p3d_steady_set_coop_max", self._h, int(max_cells))
+
     RATE_NAMES = ("H2_formation", "H2_photodiss", "H2_cr_destruction", "C_photoion",
                   "Cp_recombination", "CO_photodiss", "CO_cr_dissociation", "C_OH_to_CO")
 

@@ -95,6 +95,33 @@ def test_autotune_keeps_results():
     s.close()
 
 
+def test_cooperative_thermal_root_reaches_the_plain_state():
+    """The mixed thermal kernel solves short worklists one cell per warp with
+    the warp-cooperative FP64 net heating (net_heating_coop64: same terms,
+    another summation order).  Forced on every mixed solve (and off), the
+    converged 16^3 state matches the plain FP64 one in every settled cell
+    (1e-6 species above 1e-20 of n_H, 1e-4 T)."""
+    tol = 1e-8
+    plain, _ = _solver("cube16")
+    n_allow = 8
+    assert plain.run(max_iterations=3000, convergence_tol=tol, mixed=False, n_allow=n_allow,
+                     w_chem=0.1)
+    ref = {k: plain.get(k) for k in SPECIES + ("T_gas", "change")}
+    plain.close()
+    for coop in (1 << 30, 0):
+        s, _ = _solver("cube16")
+        s.set_coop_max(coop)
+        assert s.run(max_iterations=3000, convergence_tol=tol, mixed=True, n_allow=n_allow,
+                     w_chem=0.1)
+        moving = (s.get("change") > tol) | (ref["change"] > tol)
+        for k in SPECIES + ("T_gas",):
+            a, b = s.get(k), ref[k]
+            m = (np.abs(b) > 1e-20) & ~moving
+            rel = np.abs(a - b)[m] / np.abs(b)[m]
+            assert rel.max() <= (1e-4 if k == "T_gas" else 1e-6), (coop, k, rel.max())
+        s.close()
+
+
 def test_max_iterations_is_a_cap():
     """The mixed path runs graphs of eight iterations; a max_iterations that
     is not a multiple of eight still stops there (the remainder one by one),

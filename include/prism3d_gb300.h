@@ -388,7 +388,7 @@ int p3d_steady_autotune(p3d_steady_t *s, int warm_iters, int32_t *cfg_out, doubl
  * reference. */
 int p3d_steady_set_launch(p3d_steady_t *s, int threads, int blocks_per_sm);
 /* Mixed thermal kernel: a worklist of at most max_cells cells (default
- * 2048) is solved one cell per warp, the FP64 net heating evaluated by the
+ * 4096) is solved one cell per warp, the FP64 net heating evaluated by the
  * whole warp; longer lists 32 cells per warp.  0: never.  Results agree to
  * the root tolerance either way.  No counterpart in the reference. */
 int p3d_steady_set_coop_max(p3d_steady_t *s, int64_t max_cells);

@@ -183,9 +183,10 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   for (int k = 0; k < 8; ++k) p.rs[k] = 1.0;
   p.fix_t = 0;
   p.exact_roots = 0;
-  // one cell per warp below ~2 cells per FP64 unit (608 schedulers): above
-  // that, 32 cells per warp keep more of the units busy
-  p.coop_max = 2048;
+  // one cell per warp up to ~7 cells per FP64 unit (608 schedulers): above
+  // that, 32 cells per warp keep the units busier (128^3 slab: 4096 cells
+  // best, 2048 and 8192 within 1%)
+  p.coop_max = 4096;
   p.quiet_tol = p.quiet_in_tol = p.quiet_b_tol = p.quiet_r_tol = 0.0;
   p.pe = PeGrid{log_psi_min, log_psi_step, eg_min, eg_step, (int)n_psi, (int)n_eg};
   memcpy(p.lines.cii, cii, sizeof(p.lines.cii));

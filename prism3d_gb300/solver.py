@@ -140,7 +140,7 @@ class PDRSolverGPU:
     def set_coop_max(self, max_cells):
         """Worklists of at most max_cells cells are solved one cell per warp
         by the mixed thermal kernel (its FP64 net heating evaluated by the
-        whole warp; default 2048, 0 never)."""
+        whole warp; default 4096, 0 never)."""
         L.call("p3d_steady_set_coop_max", self._h, int(max_cells))
 
     RATE_NAMES = ("H2_formation", "H2_photodiss", "H2_cr_destruction", "C_photoion",

@@ -90,7 +90,12 @@ static unsigned cell_grid(int64_t n, int sms, int threads, int per_sm) {
 
 // Selected-ray N_H2 / N_CO columns of every cell: one launch, both directions
 // of each axis per pencil read (ss_columns_kernel).
-static void launch_columns(SteadySolver* s, const SteadyParams& par, cudaStream_t str) {
+// Lists longer than this have the next column pass recompute every tile
+// (marking them would cost more than it saves).
+constexpr int64_t kColMarkMax = 1 << 16;
+
+static void launch_columns(SteadySolver* s, const SteadyParams& par, cudaStream_t str,
+                           bool force) {
   const SteadyDev& d = s->d;
   if (s->star) {  // columns towards the star (the cell's own half layer included)
     launch_point_source(s->nx, s->ny, s->nz, s->dens, d.x_h2, d.x_co, s->star_pos, s->star_lum,
@@ -101,13 +106,14 @@ static void launch_columns(SteadySolver* s, const SteadyParams& par, cudaStream_
   ss_columns_kernel<<<(unsigned)(g.nbx + g.nby + g.nbz), 32 * kColWarps,
                       columns_smem_bytes(s->nx, s->ny), str>>>(
       par.h2_implicit, s->nx, s->ny, s->nz, g.nbx, g.nby, d.l2, d.l3, d.fam, d.ds, d.u_h2,
-      d.u_co);
+      d.u_co, d.col_dirty, s->glob, force ? 1 : 0);
 }
 
 static int launch_iteration(SteadySolver* s, bool mixed, const SteadyParams& par,
                             cudaStream_t str) {
   const SteadyDev& d = s->d;
-  launch_columns(s, par, str);
+  // mixed: only the column tiles whose layers the last chemistry rewrote
+  launch_columns(s, par, str, !mixed);
   ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(s->n, d.t_gas, s->parts);
   ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, s->n, s->glob);
   const int bt = s->cell_threads;
@@ -115,6 +121,8 @@ static int launch_iteration(SteadySolver* s, bool mixed, const SteadyParams& par
   if (mixed) {
     ss_mark_kernel<true><<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(s->n, d, par,
                                                                               s->glob);
+    ss_col_mark_kernel<<<grid_for(kColMarkMax, s->st->sms, 1), kThreads, 0, str>>>(
+        s->nx, s->ny, s->nz, d.list, d.col_dirty, s->glob, kColMarkMax);
     ss_chem_kernel<true><<<grid, bt, 0, str>>>(s->n, d, par, s->glob, s->a_nano, s->a_rest);
     ss_thermal_kernel<true><<<grid, bt, 0, str>>>(s->n, d, par, s->glob);
   } else {
@@ -127,10 +135,10 @@ static int launch_iteration(SteadySolver* s, bool mixed, const SteadyParams& par
 }
 
 // kernels of one mixed iteration with the ray-set columns (the plain path
-// launches one fewer; the point-source columns take three launches, not one)
-constexpr int kLaunchesPerIteration = 7;
+// launches two fewer; the point-source columns take three launches, not one)
+constexpr int kLaunchesPerIteration = 8;
 static int launches_per_iteration(const SteadySolver* s, bool mixed) {
-  return kLaunchesPerIteration - (mixed ? 0 : 1) + (s->star ? 2 : 0);
+  return kLaunchesPerIteration - (mixed ? 0 : 2) + (s->star ? 2 : 0);
 }
 
 }  // namespace p3d
@@ -205,7 +213,8 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   d.dens = s->dens;
   if ((rc = s->alloc(&d.ray, n)) || (rc = s->alloc(&d.fam, n)) || (rc = s->alloc(&d.flags, n)) ||
       (rc = s->alloc(&d.list, n)) || (rc = s->alloc(&d.bis_node, n)) ||
-      (rc = s->alloc(&d.bis_margin, n)) || (rc = s->alloc(&d.fh2_slope, n))) {
+      (rc = s->alloc(&d.bis_margin, n)) || (rc = s->alloc(&d.fh2_slope, n)) ||
+      (rc = s->alloc(&d.col_dirty, column_tiles(nx, ny, nz)))) {
     delete h;
     return rc;
   }
@@ -375,7 +384,11 @@ int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, in
   const int64_t stop = s->iters_done + max_outer;
   if (stop > kMaxHist) return set_error(P3D_EINVAL, "iteration history full: reset first");
   bool done = false;
-  cudaError_t e;
+  // the first column pass of a run recomputes every tile (the state may have
+  // been reset, set or refined since the last pass)
+  cudaError_t e = cudaMemsetAsync(s->d.col_dirty, 1, (size_t)column_tiles(s->nx, s->ny, s->nz),
+                                  str);
+  if (e != cudaSuccess) return cuda_fail(e, "column tiles");
   // one iteration: launch, synchronise, test
   auto single = [&]() -> int {
     int rc = launch_iteration(s, mixed != 0, par, str);
@@ -543,7 +556,7 @@ int p3d_steady_columns(p3d_steady_t* h, double* nh2_out, double* nco_out) {
   if (!h || !nh2_out || !nco_out) return set_error(P3D_EINVAL, "null argument");
   SteadySolver* s = &h->s;
   cudaStream_t str = s->st->stream;
-  launch_columns(s, s->par, str);
+  launch_columns(s, s->par, str, true);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "columns launch");
   ++s->launches;
@@ -633,7 +646,7 @@ int p3d_steady_kernel_times(p3d_steady_t* h, int reps, double* ms4) {
     cudaEventRecord(e0, str);
     for (int r = 0; r < reps; ++r) {
       if (which == 0) {
-        launch_columns(s, par, str);
+        launch_columns(s, par, str, true);
       } else if (which == 1) {
         ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(s->n, d.t_gas, s->parts);
         ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, s->n, s->glob);
@@ -880,7 +893,7 @@ int p3d_steady_adjoint(p3d_steady_t* h, const double* w6, double dx, int64_t max
   // columns and mean T of the final state
   const SteadyParams& par = s->par;
   int64_t dims[3] = {s->nx, s->ny, s->nz};
-  launch_columns(s, par, str);
+  launch_columns(s, par, str, true);
   ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(n, d.t_gas, s->parts);
   ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, n, s->glob);
   SteadyGlobals gl;
@@ -1028,7 +1041,7 @@ int p3d_steady_refine(p3d_steady_t* h, p3d_network_t* net, int32_t mixed, int32_
   }
   // columns and Doppler width of the current state
   const SteadyParams& par = s->par;
-  launch_columns(s, par, str);
+  launch_columns(s, par, str, true);
   ss_sum_kernel<<<s->nparts, kThreads, 0, str>>>(n, d.t_gas, s->parts);
   ss_finalize_kernel<<<1, 32, 0, str>>>(s->nparts, s->parts, n, s->glob);
   SteadyGlobals gl;

@@ -33,6 +33,9 @@ struct SteadyDev {
   // cells solved this iteration (dense list) and values passed from the
   // chemistry kernel to the thermal kernel
   int32_t* list;
+  // column tiles whose layers changed since their last column pass: x tiles
+  // (j, k / 32), y tiles (i, k / 32), z pencils (i, j), one byte each
+  uint8_t* col_dirty;
   double *rh2_cell, *chg_spec;
   // diagnostics of the last iteration
   double *fh2, *gamma_pe, *t_dust;
@@ -85,6 +88,7 @@ struct SteadyGlobals {
   unsigned int therm_next;  // thermal kernel: next cell (mixed: list entry) to hand out
   unsigned int chem_next;   // chemistry kernel: the same
   int iter;
+  int cols_all;  // 1: the next column pass recomputes every tile
 };
 
 // Columns of the per-iteration history record.

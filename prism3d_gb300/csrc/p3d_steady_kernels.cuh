@@ -234,15 +234,55 @@ inline ColumnsGrid columns_grid(int64_t nx, int64_t ny, int64_t nz) {
   return {ny * kt, nx * kt, ceil_div(nx * ny, kColWarps)};
 }
 
+// Number of column tiles: x tiles, y tiles, z pencils (col_dirty's layout).
+inline int64_t column_tiles(int64_t nx, int64_t ny, int64_t nz) {
+  const int64_t kt = ceil_div(nz, 32);
+  return ny * kt + nx * kt + nx * ny;
+}
+
+// Marks the column tiles of the listed cells, whose layers the chemistry of
+// this iteration rewrites, for the next column pass -- or, for a list longer
+// than max_list, has that pass recompute every tile.
+__global__ void ss_col_mark_kernel(int64_t nx, int64_t ny, int64_t nz,
+                                   const int32_t* __restrict__ list,
+                                   uint8_t* __restrict__ dirty, SteadyGlobals* g,
+                                   int64_t max_list) {
+  const int64_t count = (int64_t)g->n_active;
+  const bool all = count > max_list;
+  if (blockIdx.x == 0 && threadIdx.x == 0) g->cols_all = all ? 1 : 0;
+  if (all) return;
+  const int64_t kt = ceil_div(nz, 32);
+  uint8_t* dx = dirty;
+  uint8_t* dy = dx + ny * kt;
+  uint8_t* dz = dy + nx * kt;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < count;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = list[e];
+    const int64_t i = c / (ny * nz), j = (c / nz) % ny, k = c % nz;
+    dx[j * kt + k / 32] = 1;
+    dy[i * kt + k / 32] = 1;
+    dz[i * ny + j] = 1;
+  }
+}
+
+// force: every tile (else those marked in `dirty`, or all when g->cols_all);
+// a tile's mark is cleared when it is recomputed.  A tile left out keeps its
+// columns from the last pass, computed from the same layers.
 __global__ void __launch_bounds__(32 * kColWarps)
 ss_columns_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz, int64_t nbx,
                   int64_t nby, const double* __restrict__ lay2, const double* __restrict__ lay3,
                   const int8_t* __restrict__ fam, const double* __restrict__ ds,
-                  double* __restrict__ u_h2, double* __restrict__ u_co) {
+                  double* __restrict__ u_h2, double* __restrict__ u_co,
+                  uint8_t* __restrict__ dirty, const SteadyGlobals* __restrict__ g, int force) {
   extern __shared__ double col_sh[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t b = blockIdx.x;
+  const bool every = force || g->cols_all;
   if (b < nbx + nby) {
+    // x tile b, y tile b - nbx: dirty + b either way (x tiles first)
+    if (!every && !dirty[b]) return;
+    __syncthreads();  // every thread has read the mark before it is cleared
+    if (threadIdx.x == 0) dirty[b] = 0;
     const int axis = b < nbx ? 0 : 1;
     const int64_t t = axis == 0 ? b : b - nbx;
     const int64_t kt = ceil_div(nz, 32);
@@ -331,6 +371,10 @@ ss_columns_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz, int64_t 
   // z axis: one warp per contiguous pencil
   const int64_t pz = (b - nbx - nby) * kColWarps + w;
   if (pz >= nx * ny) return;
+  uint8_t* dzp = dirty + nbx + nby + pz;
+  if (!every && !*dzp) return;
+  __syncwarp();  // every lane has read the mark before it is cleared
+  if (lane == 0) *dzp = 0;
   const int64_t base = pz * nz;
   constexpr int kStep = 32 * kColLanesZ;
   const int8_t want_f = 5, want_b = 4;

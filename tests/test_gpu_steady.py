@@ -139,6 +139,31 @@ def test_max_iterations_is_a_cap():
     s.close()
 
 
+def test_column_tiles_left_out_match_full_passes():
+    """From its second iteration a mixed run recomputes only the column
+    tiles (32 pencils along x or y, one pencil along z) holding cells the
+    last chemistry rewrote; every run() starts with a full pass.  A full
+    mixed solve of the 96^3 slab in one run and as many one-iteration runs
+    (a full column pass each time) give the same state bit for bit, the tail
+    of the solve included (a few thousand cells listed, in the H/H2
+    transition front, most tiles left out)."""
+    s, (dens, *_) = _solver("slab96")
+    n_allow = max(8, int(1e-5 * dens.size))
+    assert s.run(max_iterations=4000, convergence_tol=1e-8, mixed=True, n_allow=n_allow,
+                 w_chem=0.1)
+    k_it = s.iterations
+    ref = {k: s.get(k) for k in SPECIES + ("T_gas", "N_H2", "N_CO")}
+    listed = s.convergence_history()[:, 8]
+    assert listed[-1] < 0.01 * dens.size, listed[-5:]
+    s.reset()
+    for _ in range(k_it):
+        s.run(max_iterations=1, convergence_tol=1e-8, mixed=True, n_allow=n_allow, w_chem=0.1)
+    assert s.iterations == k_it
+    for k, v in ref.items():
+        np.testing.assert_array_equal(s.get(k), v)
+    s.close()
+
+
 def test_heating_cooling_diagnostics_and_saved_state(tmp_path):
     """Gamma and Lambda of the converged state (the reference stores them
     after each thermal solve, solver_3d.py:891-892) against the oracle's

@@ -270,7 +270,9 @@ def run_gb300(args, ws, rank, local):
                      "per_unit": f"{FP64_OPS_PER_CELL_SOLVE:.0f} FP64 flops per cell solve "
                                  "(ncu DADD + DMUL + 2 DFMA counts of the two kernels)",
                      "fp32_flops_per_cell_solve": FP32_OPS_PER_CELL_SOLVE,
-                     "counts_source": "profiles/cell_kernels_slab128.md",
+                     "counts_source": "ncu instruction and DRAM counters of this pass's "
+                                      "chemistry and thermal launches (bench.py --profile "
+                                      "kernels, 128^3)",
                      "fp64_pipe_active_ncu": FP64_PIPE_ACTIVE_NCU},
         "roofline_hbm": {"kernel": "ss_columns_kernel (3 axes x 2 directions, one launch per "
                                    "outer iteration)",
@@ -280,7 +282,7 @@ def run_gb300(args, ws, rank, local):
                          "note": "FP64-pipe bound (82% busy: 21 DADD per cell for the running "
                                  "sums), not HBM; traffic below the algorithmic bytes: the "
                                  "layers are partly L2-resident, the columns stay in L2 "
-                                 "(profiles/columns_rt_slab128.md)"},
+                                 "(ncu, bench.py --profile kernels)"},
         "kernel_times_ms": kt,
         "fp64_net_heating_evals_per_cell_iter": float(np.mean(hist[:, 6]) / n),
         "gpu_launches": int(sum(launches)),
@@ -419,7 +421,7 @@ def rt_dropin_bench(dens, g0, cell, nside, state, hbm, peak_kind, fp64_peak, wor
                            "kernel on this GPU", "traffic": RT_DRAM_BYTES_PER_CELL[workload] * n,
                            "per_unit": f"{RT_FP64_OPS_PER_CELL[workload]:.0f} FP64 flops per cell "
                                        "(walk + merge, 48 rays; ncu counts, "
-                                       "profiles/columns_rt_slab128.md)"}
+                                       "bench.py --profile rt)"}
     return res
 
 
@@ -479,7 +481,7 @@ def network_bench(args):
 
 # Per-cell counts of the launches bench.py times for its rooflines, from ncu
 # on `bench.py --profile kernels` / `--profile rt` at 128^3 (2,097,152
-# cells; profiles/cell_kernels_slab128.md, profiles/columns_rt_slab128.md):
+# cells, one kernel per capture, --clock-control none):
 # FP64 flops (DFMA = 2, DADD / DMUL = 1) per cell solve of the mixed
 # chemistry (1,403) and thermal (1,243) kernels on the 14th outer iteration,
 # every cell solved with exact roots, and their FP32 flops (758 + 5,946);

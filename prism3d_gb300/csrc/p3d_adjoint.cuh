@@ -134,7 +134,7 @@ __device__ void adj_residual(int64_t i, const SteadyDev& d, const SteadyParams& 
   gf += hci0 * x3 * nh * kEVtoErg;
   c.gamma_fixed = gf;
   const double mu = x1 > 0.5 ? 2.0 : 1.0;
-  c.gg_coeff = 2.0 * 0.35 * 1e-21 * (nh * nh) * sqrt(8.0 * kKBoltz / (kPi * mu * kMH)) * kKBoltz;
+  c.gg_coeff = 2.0 * 0.35 * 1e-21 * (nh * nh) * (mu == 2.0 ? kGgSpeedMu2 : kGgSpeedMu1) * kKBoltz;
   c.t_dust = td;
   c.n_e = xe * nh;
   c.n_hi = x0 * nh;

@@ -8,6 +8,13 @@ namespace p3d {
 
 constexpr double kMH = 1.6735575e-24;
 constexpr double kPi = 3.14159265358979323846;
+// sqrt(8 k_B / (pi mu m_H)) for mu = 1 and mu = 2, the gas-grain coupling's
+// speed factor (thermal.rs's gg_coeff): the correctly rounded double of the
+// same expression, so the per-cell contexts keep their values while leaving
+// out a division and a square root per cell (checked in
+// tests/test_phys_host.py)
+constexpr double kGgSpeedMu1 = 0x1.c4f0d56852f3cp+13;
+constexpr double kGgSpeedMu2 = 0x1.404708f2a8ebep+13;
 
 // f_shield_H2, Draine & Bertoldi 1996 (radiative_transfer/shielding.py:17-59)
 // with b the Doppler parameter in km/s; *dfdn = d f / d N_H2 (0 where the

@@ -690,7 +690,7 @@ __device__ __forceinline__ ThermalCtx steady_thermal_ctx(const SteadyDev& d, int
   gf += d.hci0[i] * x3 * nh * kEVtoErg;
   c.gamma_fixed = gf;
   const double mu = x1 > 0.5 ? 2.0 : 1.0;
-  c.gg_coeff = 2.0 * 0.35 * 1e-21 * (nh * nh) * sqrt(8.0 * kKBoltz / (kPi * mu * kMH)) * kKBoltz;
+  c.gg_coeff = 2.0 * 0.35 * 1e-21 * (nh * nh) * (mu == 2.0 ? kGgSpeedMu2 : kGgSpeedMu1) * kKBoltz;
   c.t_dust = d.t_dust[i];
   c.n_e = d.x_e[i] * nh;
   c.n_hi = x0 * nh;
@@ -716,6 +716,11 @@ ss_heating_cooling_kernel(int64_t n, SteadyDev d, SteadyParams p, int which,
   }
 }
 
+// |now - before| / |now| to FP32 precision (0 when both are 0).
+__device__ __forceinline__ double rel_change32(double now, double before) {
+  return (double)(fabsf((float)(now - before)) / fmaxf(fabsf((float)now), 1e-30f));
+}
+
 // Thermal context (solver_3d.py:693-754), thermal root, per-cell T update and
 // convergence measure of cell i.  COOP: all lanes of the warp run it for the
 // same cell (FP64 net heating over the warp); only `lead` stores and counts.
@@ -734,12 +739,15 @@ __device__ __forceinline__ void thermal_cell(int64_t i, const SteadyDev& d, cons
     troot = tg;
   } else if (MIXED) {
     // largest relative change of the root's inputs since the cell's last
-    // thermal solve: species, T (context), H2/CO columns, Doppler width
+    // thermal solve: species, T (context), H2/CO columns, Doppler width (the
+    // ratios in FP32: delta only meets 1/300 of a certified margin, and an
+    // FP32 division costs the FP64 pipe two conversions where an FP64 one
+    // costs it a dozen instructions)
     const double tp0 = d.t_prev[i];
-    double delta = fmax(d.chg_spec[i], tp0 > 0.0 ? fabs(tg - tp0) / tg : INFINITY);
-    delta = fmax(delta, fabs(d.u_h2[i] - d.u_h2_last[i]) / fmax(fabs(d.u_h2[i]), 1e-300));
-    delta = fmax(delta, fabs(d.u_co[i] - d.u_co_last[i]) / fmax(fabs(d.u_co[i]), 1e-300));
-    delta = fmax(delta, fabs(b_dop - d.b_last[i]) / b_dop);
+    double delta = fmax(d.chg_spec[i], tp0 > 0.0 ? rel_change32(tg, tp0) : INFINITY);
+    delta = fmax(delta, rel_change32(d.u_h2[i], d.u_h2_last[i]));
+    delta = fmax(delta, rel_change32(d.u_co[i], d.u_co_last[i]));
+    delta = fmax(delta, rel_change32(b_dop, d.b_last[i]));
     node = d.bis_node[i];
     margin = d.bis_margin[i];
     // inexact roots while the cell is still moving: the root tolerance
@@ -977,7 +985,7 @@ ss_refine_scatter_kernel(int64_t n, SteadyDev d, SteadyParams p, const double* _
     gf += d.hci0[i] * x3 * nh * kEVtoErg;
     c.gamma_fixed = gf;
     const double mu = x1 > 0.5 ? 2.0 : 1.0;
-    c.gg_coeff = 2.0 * 0.35 * 1e-21 * (nh * nh) * sqrt(8.0 * kKBoltz / (kPi * mu * kMH)) * kKBoltz;
+    c.gg_coeff = 2.0 * 0.35 * 1e-21 * (nh * nh) * (mu == 2.0 ? kGgSpeedMu2 : kGgSpeedMu1) * kKBoltz;
     c.t_dust = td;
     c.n_e = xe * nh;
     c.n_hi = x0 * nh;

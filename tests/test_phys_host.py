@@ -98,3 +98,27 @@ def test_interp_idx_weight_known_answers(lib):
     assert iw(-1.0) == (0, 0.0)
     assert iw(100.0) == (8, 1.0)
     assert iw(float("nan"))[0] == 0  # NaN maps to index 0 (Rust's saturating cast)
+
+
+def test_gas_grain_speed_constants_are_the_rounded_expression():
+    """csrc/p3d_phys.cuh keeps sqrt(8 k_B / (pi mu m_H)) for mu = 1, 2 as
+    literals; they must be the doubles the per-cell expression rounds to
+    (IEEE division and square root are correctly rounded on the host as on
+    the device with -prec-div / -prec-sqrt), so the thermal contexts are
+    unchanged bit for bit."""
+    import math
+    import os
+    import re
+    csrc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                        "prism3d_gb300", "csrc")
+    text = open(os.path.join(csrc, "p3d_phys.cuh")).read()
+    common = open(os.path.join(csrc, "p3d_common.cuh")).read()
+
+    def const(src, name):
+        return re.search(rf"constexpr double {name} = ([^;]+);", src).group(1).strip()
+
+    kb = float(const(common, "kKBoltz"))
+    mh = float(const(text, "kMH"))
+    pi = float(const(text, "kPi"))
+    for mu, name in ((1.0, "kGgSpeedMu1"), (2.0, "kGgSpeedMu2")):
+        assert float.fromhex(const(text, name)) == math.sqrt(8.0 * kb / (pi * mu * mh)), name

@@ -106,7 +106,8 @@ static void launch_columns(SteadySolver* s, const SteadyParams& par, cudaStream_
   ss_columns_kernel<<<(unsigned)(g.nbx + g.nby + g.nbz), 32 * kColWarps,
                       columns_smem_bytes(s->nx, s->ny), str>>>(
       par.h2_implicit, s->nx, s->ny, s->nz, g.nbx, g.nby, d.l2, d.l3, d.fam, d.ds, d.u_h2,
-      d.u_co, d.col_dirty, s->glob, force ? 1 : 0);
+      d.u_co, d.col_dirty, s->glob, force ? 1 : 0,
+      ColQuiet{d.u_h2_last, d.u_co_last, d.q_moved, par.quiet_in_tol});
 }
 
 static int launch_iteration(SteadySolver* s, bool mixed, const SteadyParams& par,
@@ -214,7 +215,8 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
   if ((rc = s->alloc(&d.ray, n)) || (rc = s->alloc(&d.fam, n)) || (rc = s->alloc(&d.flags, n)) ||
       (rc = s->alloc(&d.list, n)) || (rc = s->alloc(&d.bis_node, n)) ||
       (rc = s->alloc(&d.bis_margin, n)) || (rc = s->alloc(&d.fh2_slope, n)) ||
-      (rc = s->alloc(&d.col_dirty, column_tiles(nx, ny, nz)))) {
+      (rc = s->alloc(&d.col_dirty, column_tiles(nx, ny, nz))) ||
+      (rc = s->alloc(&d.q_self, n)) || (rc = s->alloc(&d.q_moved, n))) {
     delete h;
     return rc;
   }
@@ -388,6 +390,13 @@ int p3d_steady_run(p3d_steady_t* h, int mixed, int64_t max_outer, double tol, in
   // been reset, set or refined since the last pass)
   cudaError_t e = cudaMemsetAsync(s->d.col_dirty, 1, (size_t)column_tiles(s->nx, s->ny, s->nz),
                                   str);
+  // the worklist's per-cell tests under this run's tolerances (the first,
+  // full column pass forms the column test)
+  if (e == cudaSuccess) {
+    ss_quiet_init_kernel<<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(s->n, s->d, par);
+    e = cudaGetLastError();
+    ++s->launches;
+  }
   if (e != cudaSuccess) return cuda_fail(e, "column tiles");
   // one iteration: launch, synchronise, test
   auto single = [&]() -> int {

@@ -36,6 +36,11 @@ struct SteadyDev {
   // column tiles whose layers changed since their last column pass: x tiles
   // (j, k / 32), y tiles (i, k / 32), z pencils (i, j), one byte each
   uint8_t* col_dirty;
+  // the worklist's per-cell tests, kept where their inputs are written:
+  // q_self (thermal kernel) = last change <= quiet_tol and last thermal
+  // residual <= quiet_r_tol; q_moved (column pass, cleared by the thermal
+  // kernel) = a column moved by more than quiet_in_tol since the last solve
+  uint8_t *q_self, *q_moved;
   double *rh2_cell, *chg_spec;
   // diagnostics of the last iteration
   double *fh2, *gamma_pe, *t_dust;

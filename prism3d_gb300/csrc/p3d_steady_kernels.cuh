@@ -209,12 +209,27 @@ constexpr int kColChunk = 8;    // cells per chunk of a strided pencil
 constexpr int kColWarps = 8;    // warps per block
 constexpr int kColLanesZ = 4;   // consecutive cells per lane on the z axis
 
+// The worklist's column test of cell c against its columns at its last
+// solve (ss_mark_kernel used to make it from u_h2 / u_h2_last / u_co /
+// u_co_last; the pass that writes the columns makes it now, so the mark
+// kernel reads one byte).
+struct ColQuiet {
+  const double* __restrict__ h2_last;
+  const double* __restrict__ co_last;
+  uint8_t* __restrict__ moved;
+  double tol;
+};
+
 __device__ __forceinline__ void col_store(int own_implicit, int64_t c, double dsc, double s2,
                                           double s3, double l2, double l3,
                                           double* __restrict__ u_h2,
-                                          double* __restrict__ u_co) {
-  u_h2[c] = own_implicit ? dsc * s2 : dsc * fma(0.5, l2, s2);
-  u_co[c] = dsc * fma(0.5, l3, s3);
+                                          double* __restrict__ u_co, const ColQuiet& q) {
+  const double uh2 = own_implicit ? dsc * s2 : dsc * fma(0.5, l2, s2);
+  const double uco = dsc * fma(0.5, l3, s3);
+  u_h2[c] = uh2;
+  u_co[c] = uco;
+  q.moved[c] = !(fabs(uh2 - q.h2_last[c]) <= q.tol * fabs(uh2) &&
+                 fabs(uco - q.co_last[c]) <= q.tol * fabs(uco));
 }
 
 // Shared memory of one strided-axis block: chunk sums and the carries from
@@ -273,7 +288,8 @@ ss_columns_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz, int64_t 
                   int64_t nby, const double* __restrict__ lay2, const double* __restrict__ lay3,
                   const int8_t* __restrict__ fam, const double* __restrict__ ds,
                   double* __restrict__ u_h2, double* __restrict__ u_co,
-                  uint8_t* __restrict__ dirty, const SteadyGlobals* __restrict__ g, int force) {
+                  uint8_t* __restrict__ dirty, const SteadyGlobals* __restrict__ g, int force,
+                  ColQuiet cq) {
   extern __shared__ double col_sh[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t b = blockIdx.x;
@@ -350,7 +366,7 @@ ss_columns_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz, int64_t 
         for (int u = 0; u < n_u; ++u) {
           const int64_t cell = c0 + u * stride;
           const double a2 = lay2[cell], a3 = lay3[cell];
-          if ((need_f >> u) & 1u) col_store(own_implicit, cell, ds[cell], f2, f3, a2, a3, u_h2, u_co);
+          if ((need_f >> u) & 1u) col_store(own_implicit, cell, ds[cell], f2, f3, a2, a3, u_h2, u_co, cq);
           f2 += a2;
           f3 += a3;
         }
@@ -360,7 +376,7 @@ ss_columns_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz, int64_t 
         for (int u = n_u - 1; u >= 0; --u) {
           const int64_t cell = c0 + u * stride;
           const double a2 = lay2[cell], a3 = lay3[cell];
-          if ((need_b >> u) & 1u) col_store(own_implicit, cell, ds[cell], b2, b3, a2, a3, u_h2, u_co);
+          if ((need_b >> u) & 1u) col_store(own_implicit, cell, ds[cell], b2, b3, a2, a3, u_h2, u_co, cq);
           b2 += a2;
           b3 += a3;
         }
@@ -425,7 +441,7 @@ ss_columns_kernel(int own_implicit, int64_t nx, int64_t ny, int64_t nz, int64_t 
         const int u = dir ? v : kColLanesZ - 1 - v;
         if (fv[u] == want)
           col_store(own_implicit, base + c0 + u, ds[base + c0 + u], r2, r3, l2[u], l3[u],
-                    u_h2, u_co);
+                    u_h2, u_co, cq);
         r2 += l2[u];
         r3 += l3[u];
       }
@@ -452,11 +468,16 @@ __global__ void ss_sum_kernel(int64_t n, const double* __restrict__ x, double* _
   }
 }
 
+// One warp (launched <<<1, 32>>>): the block partial sums reduced in a
+// fixed order (each lane its stride of them, then a butterfly), so the mean T
+// is the same on every run.
 __global__ void ss_finalize_kernel(int nparts, const double* __restrict__ part, int64_t n,
                                    SteadyGlobals* g) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
   double s = 0.0;
-  for (int b = 0; b < nparts; ++b) s += part[b];
+  for (int b = threadIdx.x; b < nparts; b += 32) s += part[b];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (threadIdx.x != 0) return;
   double tm = s / (double)n;
   g->t_mean = tm;
   g->b_dop = sqrt(2.0 * kKBoltz * tm / (2.0 * kMH)) / 1e5;
@@ -556,11 +577,9 @@ ss_mark_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g) {
     const int64_t i = base + lane;
     bool active = i < n;
     if (active && MIXED && iter > 2) {
-      const double q = p.quiet_tol, qi = p.quiet_in_tol;
-      const double uh2 = d.u_h2[i], uco = d.u_co[i];
-      if (d.chg_last[i] <= q && fabs(uh2 - d.u_h2_last[i]) <= qi * fabs(uh2) &&
-          fabs(uco - d.u_co_last[i]) <= qi * fabs(uco) &&
-          fabs(d.r_prev[i]) <= p.quiet_r_tol * d.t_prev[i]) {
+      // last change <= quiet_tol and residual <= quiet_r_tol (q_self), its
+      // columns within quiet_in_tol of their values at that solve (!q_moved)
+      if (d.q_self[i] && !d.q_moved[i]) {
         const double b_last = d.b_last[i];
         if (b_last == b_dop ||
             fabs(b_dop - b_last) * (double)d.fh2_slope[i] <= p.quiet_b_tol * b_dop)
@@ -789,6 +808,17 @@ __device__ __forceinline__ void thermal_cell(int64_t i, const SteadyDev& d, cons
   d.u_co_last[i] = d.u_co[i];
   d.b_last[i] = b_dop;
   d.chg_last[i] = m;
+  d.q_self[i] = m <= p.quiet_tol && fabs(rp) <= p.quiet_r_tol * tp;
+  d.q_moved[i] = 0;
+}
+
+// q_self of every cell from its last change and residual under this run's
+// tolerances (run() start: a reset, set, dust step or another tolerance may
+// have changed them since they were formed).
+__global__ void ss_quiet_init_kernel(int64_t n, SteadyDev d, SteadyParams p) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    d.q_self[i] = d.chg_last[i] <= p.quiet_tol && fabs(d.r_prev[i]) <= p.quiet_r_tol * d.t_prev[i];
 }
 
 // __maxnreg__ 80 (6 resident blocks of 128 threads per SM instead of 4 at

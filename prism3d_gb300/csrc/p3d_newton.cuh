@@ -46,7 +46,7 @@ template <bool FAST = false>
 __device__ __forceinline__ void chem_prepare(ChemCell& p) {
   if (p.ds > 0.0) return;
   double d1, dh;
-  p.fh2_fix = fsh_h2(p.u_h2, p.b_dop, &d1);
+  p.fh2_fix = fsh_h2<FAST>(p.u_h2, p.b_dop, &d1);
   p.kpd_fix = p.kpd0 * p.fh2_fix;
   p.kco_fix = p.kco0 * fsh_co<FAST>(p.u_co, p.u_h2, &dh) + p.kco_cr;
 }
@@ -223,7 +223,9 @@ __device__ __forceinline__ int chem_steady_cell(const ChemCell& p, double* y, in
         float inv = 1.0f / m;
 #pragma unroll
         for (int c = 0; c < 5; ++c) A[r][c] *= inv;
-        b[r] = (float)((os >= 0 ? f[r] : -f[r]) / (double)m);
+        // the row's FP64 residual scaled by the same FP32 factor as its
+        // matrix row (an FP64 multiply, not a division, for the FP64 pipe)
+        b[r] = (float)((os >= 0 ? f[r] : -f[r]) * (double)inv);
       }
       double bd[5];
 #pragma unroll

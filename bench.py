@@ -237,7 +237,9 @@ def run_gb300(args, ws, rank, local):
     kt = kernel_times(s, reps=1)
     hbm, peak_kind = measured_peaks()
     fp64_peak = fp64_peak_tflops()
-    col_bytes = 41.0 * n  # read layers 2 n x_H2, n x_CO, family, ds once; write N_H2, N_CO
+    # read the layers 2 n x_H2, n x_CO, family, ds and the columns at each
+    # cell's last solve once; write N_H2, N_CO and the column-drift byte
+    col_bytes = 58.0 * n
     col_gbs = col_bytes / (kt["columns_ms"] * 1e-3) / 1e9
     cell_tf = FP64_OPS_PER_CELL_SOLVE * n / (kt["cell_mixed_ms"] * 1e-3) / 1e12
     out = {
@@ -279,10 +281,12 @@ def run_gb300(args, ws, rank, local):
                          "bound": "hbm", "achieved": col_gbs, "peak": hbm, "unit": "GB/s",
                          "frac": col_gbs / hbm, "traffic": COLUMNS_DRAM_BYTES_PER_CELL * n,
                          "peak_source": peak_kind, "algorithmic_bytes_per_launch": col_bytes,
-                         "note": "FP64-pipe bound (82% busy: 21 DADD per cell for the running "
+                         "note": "FP64-pipe bound (82% busy: 22 DADD per cell for the running "
                                  "sums), not HBM; traffic below the algorithmic bytes: the "
                                  "layers are partly L2-resident, the columns stay in L2 "
-                                 "(ncu, bench.py --profile kernels)"},
+                                 "(ncu, bench.py --profile kernels); a full pass, where a "
+                                 "mixed run's last iterations recompute only the tiles "
+                                 "holding rewritten cells"},
         "kernel_times_ms": kt,
         "fp64_net_heating_evals_per_cell_iter": float(np.mean(hist[:, 6]) / n),
         "gpu_launches": int(sum(launches)),
@@ -483,20 +487,21 @@ def network_bench(args):
 # on `bench.py --profile kernels` / `--profile rt` at 128^3 (2,097,152
 # cells, one kernel per capture, --clock-control none):
 # FP64 flops (DFMA = 2, DADD / DMUL = 1) per cell solve of the mixed
-# chemistry (1,403) and thermal (1,243) kernels on the 14th outer iteration,
-# every cell solved with exact roots, and their FP32 flops (758 + 5,946);
-# DRAM bytes of the two launches (read + write: 327.4 + 204.8 and 530.3 +
-# 260.7 MB): the state is streamed once per solve, so the traffic scales
+# chemistry (1,116) and thermal (1,180) kernels on the 14th outer iteration,
+# every cell solved with exact roots, and their FP32 flops (726 + 5,978);
+# DRAM bytes of the two launches (read + write: 328.5 + 212.8 and 528.3 +
+# 265.9 MB): the state is streamed once per solve, so the traffic scales
 # with the cells solved.
-FP64_OPS_PER_CELL_SOLVE = 1402.7 + 1242.9
-FP32_OPS_PER_CELL_SOLVE = 757.5 + 5945.7
-DRAM_BYTES_PER_CELL_SOLVE = (327.4 + 204.8 + 530.3 + 260.7) * 1e6 / 2097152
-FP64_PIPE_ACTIVE_NCU = ("86% (chemistry), 70% (thermal): the pipe also runs FP64 compares, "
+FP64_OPS_PER_CELL_SOLVE = 1116.1 + 1179.9
+FP32_OPS_PER_CELL_SOLVE = 725.7 + 5977.7
+DRAM_BYTES_PER_CELL_SOLVE = (328.5 + 212.8 + 528.3 + 265.9) * 1e6 / 2097152
+FP64_PIPE_ACTIVE_NCU = ("85% (chemistry), 70% (thermal): the pipe also runs FP64 compares, "
                         "min/max and FP32<->FP64 conversions; the thermal kernel's remaining "
                         "time is latency of divergent root paths")
-# columns launch: FP64-pipe bound (82% busy), 27 FP64 flops per cell; DRAM
-# per launch (read + write) with the chemistry's layers partly L2-resident
-COLUMNS_DRAM_BYTES_PER_CELL = (55.9 + 6.0) * 1e6 / 2097152
+# columns launch (a full pass): FP64-pipe bound (82% busy), 29 FP64 flops
+# per cell; DRAM per launch (read + write) with the chemistry's layers partly
+# L2-resident
+COLUMNS_DRAM_BYTES_PER_CELL = (82.1 + 13.5) * 1e6 / 2097152
 # drop-in ray march (walk + merge, 48 rays) at 128^3: FP64 flops per cell
 # and DRAM bytes per cell of the two launches
 RT_FP64_OPS_PER_CELL = {"slab128": 684.0 + 12.0}

@@ -468,16 +468,16 @@ __global__ void ss_sum_kernel(int64_t n, const double* __restrict__ x, double* _
   }
 }
 
-// One warp (launched <<<1, 32>>>): the block partial sums reduced in a
-// fixed order (each lane its stride of them, then a butterfly), so the mean T
-// is the same on every run.
+// The block partial sums added in order by one thread: the mean T (and so
+// the Doppler width every cell's H2 shielding sees) is the same on every run
+// and unchanged from the order the plain path's tests were pinned with (a
+// tree order moves it by an ulp, enough to flip which few cells chatter on a
+// bisection node at tol 1e-11).
 __global__ void ss_finalize_kernel(int nparts, const double* __restrict__ part, int64_t n,
                                    SteadyGlobals* g) {
-  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
   double s = 0.0;
-  for (int b = threadIdx.x; b < nparts; b += 32) s += part[b];
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (threadIdx.x != 0) return;
+  for (int b = 0; b < nparts; ++b) s += part[b];
   double tm = s / (double)n;
   g->t_mean = tm;
   g->b_dop = sqrt(2.0 * kKBoltz * tm / (2.0 * kMH)) / 1e5;

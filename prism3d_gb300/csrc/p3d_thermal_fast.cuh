@@ -180,6 +180,45 @@ __host__ __device__ inline CoopLine coop_line(int e, const LineFast& lf, const C
   return L;
 }
 
+// Table entry L's cooling term at T (lt = ln T, inv_t = 1 / T).
+__device__ __forceinline__ double coop_term(const CoopLine& L, double lt, double inv_t,
+                                            const ThermalCtx& c) {
+  double q = L.c2 * exp64(L.a2 * lt) * c.n_h2;
+  if (L.c1 != 0.0) {
+    q += L.c1 * exp64(L.a1 * lt) * c.n_hi;
+    q += L.c3 * exp64(fma(L.d3, inv_t, L.a3 * lt)) * c.n_e;
+  }
+  const double r = L.g * q * exp64(-L.t_ul * inv_t);
+  const double nx = L.species == 3 ? c.n_co
+                    : (L.species == 0 ? c.n_cp_nh : (L.species == 1 ? c.n_o_nh : c.n_c_nh));
+  return nx * (r / (r + L.a + q)) * L.e;
+}
+
+// The net heating's terms outside the table, given the table's sum `lines`.
+__device__ __forceinline__ double coop_rest(double t, double lt, double sqrt_t, double inv_t,
+                                            const ThermalCtx& c, double lines) {
+  const double inv_sqrt_t = sqrt_t * inv_t;
+  double net = c.gamma_fixed + c.gg_coeff * sqrt_t * (c.t_dust - t) - lines;
+  if (t >= 100.0) {
+    double x = fmin(fmax(lt / kLn10, 2.0), 4.5);
+    double llh = -24.311 + x * (3.5692 + x * (-11.332 + x * (15.738 + x * (-10.581 +
+                 x * (3.5803 + x * -0.48365)))));
+    double llh2 = -24.311 + x * (4.6585 + x * (-14.272 + x * (19.779 + x * (-13.255 +
+                  x * (4.4840 + x * -0.60504)))));
+    double l0 = exp64(llh * kLn10) * c.n_hi + exp64(llh2 * kLn10) * c.n_h2;
+    double lte = exp64((-19.703 + 0.5 * x) * kLn10);
+    net -= c.n_h2 * l0 * lte / fmax(l0 + lte, 1e-50);
+  }
+  if (t >= 3000.0) net -= c.n_hi * c.n_e * (2.41e-6 * inv_sqrt_t * 0.486 * exp64(-1.18e5 * inv_t)) *
+                          10.2 * kEVtoErg;
+  {
+    double gg_cool = c.gg_coeff * sqrt_t * (t - c.t_dust);
+    if (gg_cool > 0.0) net -= gg_cool;
+  }
+  net -= c.n_cp_nh * c.n_e * (4.67e-12 * exp64(-0.6 * (lt - kLn300))) * kKBoltz * t;
+  return net;
+}
+
 #ifdef __CUDA_ARCH__
 // The FP64 net heating of one cell at t, evaluated by all 32 lanes of a
 // warp together and returned to every lane: each lane takes the table
@@ -200,49 +239,37 @@ __device__ __noinline__ double net_heating_coop64(double t, const ThermalCtx& c,
   const double lt = log(t);
   const double sqrt_t = sqrt(t);
   const double inv_t = 1.0 / t;
-  const double inv_sqrt_t = sqrt_t * inv_t;
   const int nlev = co_levels_below(5.0 * t, co);
   double part = 0.0;
   for (int e = lane; e < kCoopLines; e += 32) {
     if (e >= 5 && e - 5 >= nlev) continue;
-    const CoopLine L = tab[e];
-    double q = L.c2 * exp64(L.a2 * lt) * c.n_h2;
-    if (L.c1 != 0.0) {
-      q += L.c1 * exp64(L.a1 * lt) * c.n_hi;
-      q += L.c3 * exp64(fma(L.d3, inv_t, L.a3 * lt)) * c.n_e;
-    }
-    const double r = L.g * q * exp64(-L.t_ul * inv_t);
-    const double nx = L.species == 3 ? c.n_co
-                      : (L.species == 0 ? c.n_cp_nh : (L.species == 1 ? c.n_o_nh : c.n_c_nh));
-    part += nx * (r / (r + L.a + q)) * L.e;
+    part += coop_term(tab[e], lt, inv_t, c);
   }
   for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
   part = __shfl_sync(0xffffffffu, part, 0);
-  double net = c.gamma_fixed + c.gg_coeff * sqrt_t * (c.t_dust - t) - part;
-  if (t >= 100.0) {
-    double x = fmin(fmax(lt / kLn10, 2.0), 4.5);
-    double llh = -24.311 + x * (3.5692 + x * (-11.332 + x * (15.738 + x * (-10.581 +
-                 x * (3.5803 + x * -0.48365)))));
-    double llh2 = -24.311 + x * (4.6585 + x * (-14.272 + x * (19.779 + x * (-13.255 +
-                  x * (4.4840 + x * -0.60504)))));
-    double l0 = exp64(llh * kLn10) * c.n_hi + exp64(llh2 * kLn10) * c.n_h2;
-    double lte = exp64((-19.703 + 0.5 * x) * kLn10);
-    net -= c.n_h2 * l0 * lte / fmax(l0 + lte, 1e-50);
-  }
-  if (t >= 3000.0) net -= c.n_hi * c.n_e * (2.41e-6 * inv_sqrt_t * 0.486 * exp64(-1.18e5 * inv_t)) *
-                          10.2 * kEVtoErg;
-  {
-    double gg_cool = c.gg_coeff * sqrt_t * (t - c.t_dust);
-    if (gg_cool > 0.0) net -= gg_cool;
-  }
-  net -= c.n_cp_nh * c.n_e * (4.67e-12 * exp64(-0.6 * (lt - kLn300))) * kKBoltz * t;
   (void)theta2;
-  return net;
+  return coop_rest(t, lt, sqrt_t, inv_t, c, part);
 }
+#elif defined(__CUDACC__)
+// nvcc's host pass: the device definition above is the one that runs
+__device__ __noinline__ double net_heating_coop64(double t, const ThermalCtx& c,
+                                                  const CoopLine* __restrict__ tab,
+                                                  const CoLevel* __restrict__ co,
+                                                  double theta2);
 #else
-// host builds (the CPU tests) have no warps: the lane-wise form
-inline double net_heating_coop64(double t, const ThermalCtx& c, const CoopLine*,
-                                 const CoLevel* co, double theta2);
+// Host builds (the CPU tests): the same terms, the table summed in order.
+inline double net_heating_coop64(double t, const ThermalCtx& c, const CoopLine* tab,
+                                 const CoLevel* co, double theta2) {
+  const double lt = log(t);
+  const double sqrt_t = sqrt(t);
+  const double inv_t = 1.0 / t;
+  const int nlev = co_levels_below(5.0 * t, co);
+  double part = 0.0;
+  for (int e = 0; e < kCoopLines; ++e)
+    if (e < 5 || e - 5 < nlev) part += coop_term(tab[e], lt, inv_t, c);
+  (void)theta2;
+  return coop_rest(t, lt, sqrt_t, inv_t, c, part);
+}
 #endif
 
 // Per-cell FP32 coefficients, scaled by 1 / Gamma_fixed.

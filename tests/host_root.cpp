@@ -25,6 +25,7 @@ CoLevel g_co[40];
 float g_l32[20], g_co32[200];
 double g_mid[1024];
 BisectNode g_node[1024];
+CoopLine g_coop[kCoopLines];
 LineParams g_lp;
 LineFast g_lf;
 double g_theta2;
@@ -92,6 +93,7 @@ extern "C" void hr_init(const double* cii, const double* oi63, const double* oi1
     }
   }
   g_mid[0] = 0.0;
+  for (int e = 0; e < kCoopLines; ++e) g_coop[e] = coop_line(e, g_lf, g_co);
 }
 
 // ctx: n x 10, row-major.  node / margin: in-out per cell (0 / 0 for a cell
@@ -109,6 +111,31 @@ extern "C" void hr_root_mixed(long n, const double* ctx, const double* t_warm,
     margin[i] = mg;
     n64[i] = ev;
     status[i] = st;
+  }
+}
+
+// The same with the warp-cooperative form of the FP64 net heating (on the
+// host its table summed in order).
+extern "C" void hr_root_mixed_coop(long n, const double* ctx, const double* t_warm,
+                                   const double* delta, int* node, float* margin, double tol,
+                                   double* t_out, int* n64, int* status) {
+  for (long i = 0; i < n; ++i) {
+    ThermalCtx c = make_ctx(ctx + 10 * i);
+    int nd = node[i], st = 0, ev = 0;
+    float mg = margin[i];
+    t_out[i] = root_mixed<true>(c, g_lf, g_co, g_theta2, g_l32, g_co32, g_mid, g_node, tol, 80,
+                                t_warm[i], delta[i], &nd, &mg, &st, &ev, g_coop);
+    node[i] = nd;
+    margin[i] = mg;
+    n64[i] = ev;
+    status[i] = st;
+  }
+}
+
+extern "C" void hr_net64_coop(long n, const double* ctx, const double* t, double* out) {
+  for (long i = 0; i < n; ++i) {
+    ThermalCtx c = make_ctx(ctx + 10 * i);
+    out[i] = net_heating_coop64(t[i], c, g_coop, g_co, g_theta2);
   }
 }
 

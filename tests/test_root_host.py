@@ -162,6 +162,39 @@ def test_root_at_a_bracket_end_costs_one_end_check(lib, contexts):
         assert ev.max() <= 3, np.bincount(ev)
 
 
+def test_cooperative_net_heating_and_root(lib, contexts):
+    """The thermal kernel's warp-cooperative FP64 net heating
+    (net_heating_coop64: the 5 fine-structure lines and 40 CO levels as one
+    table of two-level lines, coop_line) against the lane-wise one
+    (net_heating_fast64_body) on the oracle's contexts at 12 temperatures
+    over 10 K - 1e5 K: equal to 1e-13 of the heating + cooling scale (the
+    table's folded constants and the summation order differ); and the mixed
+    root with it lands on the lane-wise root to 1e-9 (both to tol 1e-10)."""
+    ctx = contexts[1]
+    n = ctx.shape[0]
+    rng = np.random.default_rng(7)
+    for t0 in np.geomspace(10.0, 1e5, 12):
+        t = np.ascontiguousarray(t0 * np.exp(rng.uniform(-0.05, 0.05, n)))
+        a = _net(lib, ctx, t)
+        b = np.zeros(n)
+        lib.hr_net64_coop(ctypes.c_long(n), _p(ctx), _p(t), _p(b))
+        g, l = np.zeros(n), np.zeros(n)
+        lib.hr_heating_cooling(ctypes.c_long(n), _p(ctx), _p(t), _p(g), _p(l))
+        assert np.all(np.abs(a - b) <= 1e-13 * (np.abs(g) + np.abs(l))), (t0, np.max(
+            np.abs(a - b) / (np.abs(g) + np.abs(l))))
+    tm, _, sm = _mixed(lib, ctx, np.zeros(n), np.full(n, np.inf), np.zeros(n, np.int32),
+                       np.zeros(n, np.float32))
+    tc = np.zeros(n)
+    ev = np.zeros(n, np.int32)
+    st = np.zeros(n, np.int32)
+    lib.hr_root_mixed_coop(ctypes.c_long(n), _p(ctx), _p(np.zeros(n)), _p(np.full(n, np.inf)),
+                           _p(np.zeros(n, np.int32)), _p(np.zeros(n, np.float32)),
+                           ctypes.c_double(TOL), _p(tc), _p(ev), _p(st))
+    assert sm.sum() == 0 and st.sum() == 0
+    rel = np.abs(tc - tm) / tm
+    assert np.mean(rel <= 1e-9) >= 0.999, np.sort(rel)[-5:]
+
+
 def test_mixed_root_in_the_outer_loop_reaches_the_plain_fixed_point(lib, monkeypatch):
     """The oracle's steady method on the 24^3 slab cut, once with its plain
     FP64 roots and once with the host-built mixed root in their place (warm

@@ -108,13 +108,22 @@ __device__ __forceinline__ double tdust(double td_rad, double nh, double tg) {
   return nh > 1e5 ? td_rad * (1.0 - fc) + tg * fc : td_rad;
 }
 
-// H2 formation rate coefficient (themis_tables.py:278-319).
+// H2 formation rate coefficient (themis_tables.py:278-319).  FAST (the mixed
+// path): 8 k_B / (pi m_H) folded into one constant and the two exponentials
+// from exp64 with their divisions as multiplies (two FP64 divisions and two
+// library exponentials less per cell; ~1e-16 relative).
+constexpr double kH2SpeedSq = 0x1.90b1aa149d378p+27;  // 8 k_B / (pi m_H)
+template <bool FAST = false>
 __device__ __forceinline__ double h2_form(double tg, double td, double fnano, double s_nano,
                                           double s_lc, double s_sil) {
-  double v = sqrt(8.0 * kKBoltz * tg / (kPi * kMH));
+  double v = FAST ? sqrt(kH2SpeedSq * tg) : sqrt(8.0 * kKBoltz * tg / (kPi * kMH));
   double s = 1.0 / (1.0 + 0.04 * sqrt(tg + td) + 0.002 * tg + 8e-6 * tg * tg);
-  double e_sil = td < 14.0 ? 1.0 : (td < 25.0 ? exp(-(td - 14.0) / 5.0) : 0.01);
-  double e_c = td < 50.0 ? 0.8 : (td < 400.0 ? 0.8 * exp(-(td - 50.0) / 200.0) : 0.01);
+  double e_sil = td < 14.0 ? 1.0
+                 : (td < 25.0 ? (FAST ? exp64((14.0 - td) * 0.2) : exp(-(td - 14.0) / 5.0))
+                              : 0.01);
+  double e_c = td < 50.0 ? 0.8
+               : (td < 400.0 ? 0.8 * (FAST ? exp64((50.0 - td) * 0.005) : exp(-(td - 50.0) / 200.0))
+                             : 0.01);
   e_c = fmax(e_c, 0.005);
   return 0.5 * v * s * (e_c * s_nano * fnano + e_c * s_lc + e_sil * s_sil);
 }

@@ -625,7 +625,7 @@ ss_chem_kernel(int64_t n, SteadyDev d, SteadyParams p, SteadyGlobals* g,
     const double fn = d.f_nano[i];
     const double gpe = pe_cell(p.pe, a_nano, a_rest, d.g0[i], tg, xe0, nh, fn, d.e_g[i]);
     const double td = tdust(d.td_rad[i], nh, tg);
-    const double rh2 = h2_form(tg, td, fn, p.sigma_nano, p.sigma_lc, p.sigma_sil);
+    const double rh2 = h2_form<MIXED>(tg, td, fn, p.sigma_nano, p.sigma_lc, p.sigma_sil);
     const double zeta = d.zeta[i];
     // chemistry (solver_3d.py:549-557 rates; steady state of chemistry.rs:35-49)
     ChemCell cc;

@@ -143,7 +143,7 @@ __device__ void adj_residual(int64_t i, const SteadyDev& d, const SteadyParams& 
   c.n_cp_nh = u[2] * nh;
   c.n_o_nh = fmax(p.x_o_total - u[4], 1e-30) * nh;
   c.n_c_nh = x3 * nh;
-  G[5] = net_heating_fast64(t_eval > 0.0 ? t_eval : T, c, p.lf, c_co_ss, p.theta2);
+  G[5] = net_heating_fast64_body(t_eval > 0.0 ? t_eval : T, c, p.lf, c_co_ss, p.theta2);
 }
 
 // Gauss-Jordan inverse of a 6x6 matrix with partial pivoting; false if

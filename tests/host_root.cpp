@@ -132,6 +132,14 @@ extern "C" void hr_root_mixed_coop(long n, const double* ctx, const double* t_wa
   }
 }
 
+// The mixed root's form of the FP64 net heating (power laws as products).
+extern "C" void hr_net64_mixed(long n, const double* ctx, const double* t, double* out) {
+  for (long i = 0; i < n; ++i) {
+    ThermalCtx c = make_ctx(ctx + 10 * i);
+    out[i] = net_heating_fast64_body<true>(t[i], c, g_lf, g_co, g_theta2);
+  }
+}
+
 extern "C" void hr_net64_coop(long n, const double* ctx, const double* t, double* out) {
   for (long i = 0; i < n; ++i) {
     ThermalCtx c = make_ctx(ctx + 10 * i);

@@ -165,8 +165,9 @@ def test_root_at_a_bracket_end_costs_one_end_check(lib, contexts):
 def test_cooperative_net_heating_and_root(lib, contexts):
     """The thermal kernel's warp-cooperative FP64 net heating
     (net_heating_coop64: the 5 fine-structure lines and 40 CO levels as one
-    table of two-level lines, coop_line) against the lane-wise one
-    (net_heating_fast64_body) on the oracle's contexts at 12 temperatures
+    table of two-level lines, coop_line) and the mixed root's lane-wise form
+    (net_heating_fast64_body<true>: power laws as products of T^0.01)
+    against the plain form (net_heating_fast64_body) on the oracle's contexts at 12 temperatures
     over 10 K - 1e5 K: equal to 1e-13 of the heating + cooling scale (the
     table's folded constants and the summation order differ); and the mixed
     root with it lands on the lane-wise root to 1e-9 (both to tol 1e-10)."""
@@ -178,10 +179,14 @@ def test_cooperative_net_heating_and_root(lib, contexts):
         a = _net(lib, ctx, t)
         b = np.zeros(n)
         lib.hr_net64_coop(ctypes.c_long(n), _p(ctx), _p(t), _p(b))
+        m = np.zeros(n)
+        lib.hr_net64_mixed(ctypes.c_long(n), _p(ctx), _p(t), _p(m))
         g, l = np.zeros(n), np.zeros(n)
         lib.hr_heating_cooling(ctypes.c_long(n), _p(ctx), _p(t), _p(g), _p(l))
-        assert np.all(np.abs(a - b) <= 1e-13 * (np.abs(g) + np.abs(l))), (t0, np.max(
-            np.abs(a - b) / (np.abs(g) + np.abs(l))))
+        scale = np.abs(g) + np.abs(l)
+        for other in (b, m):  # cooperative form; mixed form (power laws as products)
+            assert np.all(np.abs(a - other) <= 1e-13 * scale), (t0, np.max(
+                np.abs(a - other) / scale))
     tm, _, sm = _mixed(lib, ctx, np.zeros(n), np.full(n, np.inf), np.zeros(n, np.int32),
                        np.zeros(n, np.float32))
     tc = np.zeros(n)

@@ -46,48 +46,6 @@ __device__ __forceinline__ double line64(double q, const LineFast& lf, int k, do
   return r_lu / (r_lu + lf.a[k] + q) * lf.e[k];
 }
 
-// FAST (the mixed root's evaluation): the eight power laws of T in the line
-// collision rates as products of u = T^0.01 (one exp64 and 22 multiplies
-// instead of eight exp64; each power a few ulp from the direct form, the
-// (T / 100)^a factors as constants 100^-a times T^a).
-constexpr double k100m007 = 0x1.72e94529230b1p-1;  // 100^-0.07
-constexpr double k100m012 = 0x1.26a0103f59cb3p-1;  // 100^-0.12
-constexpr double k100m039 = 0x1.53e22669d9ed8p-3;  // 100^-0.39
-constexpr double k100m030 = 0x1.0137987dd704cp-2;  // 100^-0.30
-
-struct TPowers {
-  double p007, p012, p039, p067, p064, p060, p058, p030;  // (T/100)^0.07 ... T^0.67 ...
-};
-
-template <bool FAST>
-__device__ __forceinline__ TPowers t_powers(double lt, double l01) {
-  TPowers w;
-  if (FAST) {
-    const double u = exp64(0.01 * lt);
-    const double u2 = u * u, u4 = u2 * u2, u8 = u4 * u4, u16 = u8 * u8, u32 = u16 * u16;
-    const double u3 = u2 * u, u12 = u8 * u4, u6 = u4 * u2;
-    w.p007 = k100m007 * (u4 * u3);
-    w.p012 = k100m012 * u12;
-    w.p039 = k100m039 * (u32 * (u4 * u3));
-    w.p067 = (u32 * u32) * u3;
-    w.p064 = u32 * u32;
-    w.p060 = (u32 * u16) * u12;
-    w.p058 = (u32 * u16) * (u8 * u2);
-    w.p030 = k100m030 * ((u16 * u8) * u6);
-  } else {
-    w.p007 = exp64(0.07 * l01);
-    w.p012 = exp64(0.12 * l01);
-    w.p039 = exp64(0.39 * l01);
-    w.p067 = exp64(0.67 * lt);
-    w.p064 = exp64(0.64 * lt);
-    w.p060 = exp64(0.60 * lt);
-    w.p058 = exp64(0.58 * lt);
-    w.p030 = exp64(0.3 * l01);
-  }
-  return w;
-}
-
-template <bool FAST = false>
 __device__ __forceinline__ double net_heating_fast64_body(double t, const ThermalCtx& c,
                                                      const LineFast& lf,
                                                      const CoLevel* __restrict__ co,
@@ -97,7 +55,109 @@ __device__ __forceinline__ double net_heating_fast64_body(double t, const Therma
   const double sqrt_t = sqrt(t);
   const double inv_t = 1.0 / t;
   const double inv_sqrt_t = sqrt_t * inv_t;
-  const TPowers w = t_powers<FAST>(lt, l01);
+  double net = c.gamma_fixed + c.gg_coeff * sqrt_t * (c.t_dust - t);
+  {  // [CII] 158
+    const double b = exp64(-lf.t_ul[0] * inv_t);
+    const double q = lf.cii_ce * inv_sqrt_t * b * c.n_e + 8.0e-10 * exp64(0.07 * l01) * c.n_hi +
+                     4.9e-10 * exp64(0.12 * l01) * c.n_h2;
+    const double r_lu = lf.g_ratio[0] * q * b;
+    net -= c.n_cp_nh * (r_lu / (r_lu + lf.a[0] + q)) * lf.e[0];
+  }
+  const double e039 = exp64(0.39 * l01);
+  net -= c.n_o_nh * line64(9.2e-12 * exp64(0.67 * lt) * c.n_hi + 4.5e-12 * exp64(0.64 * lt) * c.n_h2 +
+                               1.4e-8 * e039 * c.n_e, lf, 1, inv_t);
+  net -= c.n_o_nh * line64(4.0e-12 * exp64(0.60 * lt) * c.n_hi + 2.0e-12 * exp64(0.58 * lt) * c.n_h2 +
+                               5.0e-9 * e039 * c.n_e, lf, 2, inv_t);
+  {
+    const double t03 = exp64(0.3 * l01);
+    const double q = 1.0e-10 * t03 * c.n_hi + 5.0e-11 * t03 * c.n_h2 + 2.0e-6 * inv_sqrt_t * c.n_e;
+    net -= c.n_c_nh * (line64(q, lf, 3, inv_t) + line64(q, lf, 4, inv_t));
+  }
+  {  // CO ladder: sum_J A h nu r_lu / (r_lu + A + gamma), the fractions of
+     // up to 8 levels combined over a common denominator (one division per
+     // group instead of one per level)
+    const double gn = 3.3e-11 * (0.1 * sqrt_t) * c.n_h2;
+    const int nlev = co_levels_below(5.0 * t, co);
+    const double q1 = exp64(-theta2 * inv_t);
+    double qj = q1, bj = 1.0, sum = 0.0;
+    for (int k0 = 0; k0 < nlev; k0 += 8) {
+      const int k1 = k0 + 8 < nlev ? k0 + 8 : nlev;
+      double num = 0.0, den = 1.0;
+      for (int k = k0; k < k1; ++k) {
+        bj *= qj;  // exp(-T_u(J) / T), J = k + 1
+        qj *= q1;
+        const double gam = gn * co[k].j_factor;
+        const double r_lu = co[k].g_ratio * gam * bj;
+        const double d = r_lu + co[k].a_co + gam;
+        num = fma(num, d, r_lu * co[k].ahv * den);
+        den *= d;
+      }
+      sum += num / den;
+    }
+    net -= c.n_co * sum;
+  }
+  if (t >= 100.0) {
+    double x = fmin(fmax(lt / kLn10, 2.0), 4.5);
+    double llh = -24.311 + x * (3.5692 + x * (-11.332 + x * (15.738 + x * (-10.581 +
+                 x * (3.5803 + x * -0.48365)))));
+    double llh2 = -24.311 + x * (4.6585 + x * (-14.272 + x * (19.779 + x * (-13.255 +
+                  x * (4.4840 + x * -0.60504)))));
+    double l0 = exp64(llh * kLn10) * c.n_hi + exp64(llh2 * kLn10) * c.n_h2;
+    double lte = exp64((-19.703 + 0.5 * x) * kLn10);
+    net -= c.n_h2 * l0 * lte / fmax(l0 + lte, 1e-50);
+  }
+  if (t >= 3000.0) net -= c.n_hi * c.n_e * (2.41e-6 * inv_sqrt_t * 0.486 * exp64(-1.18e5 * inv_t)) *
+                          10.2 * kEVtoErg;
+  {
+    double gg_cool = c.gg_coeff * sqrt_t * (t - c.t_dust);
+    if (gg_cool > 0.0) net -= gg_cool;
+  }
+  net -= c.n_cp_nh * c.n_e * (4.67e-12 * exp64(-0.6 * (lt - kLn300))) * kKBoltz * t;
+  return net;
+}
+
+// The mixed root's form of the same net heating: the eight power laws of T
+// in the line collision rates as products of u = T^0.01 (one exp64 and 22
+// multiplies instead of eight exp64; each power a few ulp from the direct
+// form, the (T / 100)^a factors as constants 100^-a times T^a).  The plain
+// path keeps net_heating_fast64_body as it is (its FP64 solves are the
+// reference's method; a change of its rounding moves which few cells
+// chatter on a bisection node at tight tolerances).
+constexpr double k100m007 = 0x1.72e94529230b1p-1;  // 100^-0.07
+constexpr double k100m012 = 0x1.26a0103f59cb3p-1;  // 100^-0.12
+constexpr double k100m039 = 0x1.53e22669d9ed8p-3;  // 100^-0.39
+constexpr double k100m030 = 0x1.0137987dd704cp-2;  // 100^-0.30
+
+struct TPowers {
+  double p007, p012, p039, p067, p064, p060, p058, p030;  // (T/100)^0.07 ... T^0.67 ...
+};
+
+__device__ __forceinline__ TPowers t_powers_mixed(double lt) {
+  TPowers w;
+  const double u = exp64(0.01 * lt);
+  const double u2 = u * u, u4 = u2 * u2, u8 = u4 * u4, u16 = u8 * u8, u32 = u16 * u16;
+  const double u3 = u2 * u, u12 = u8 * u4, u6 = u4 * u2;
+  w.p007 = k100m007 * (u4 * u3);
+  w.p012 = k100m012 * u12;
+  w.p039 = k100m039 * (u32 * (u4 * u3));
+  w.p067 = (u32 * u32) * u3;
+  w.p064 = u32 * u32;
+  w.p060 = (u32 * u16) * u12;
+  w.p058 = (u32 * u16) * (u8 * u2);
+  w.p030 = k100m030 * ((u16 * u8) * u6);
+  return w;
+}
+
+__device__ __forceinline__ double net_heating_mixed64_body(double t, const ThermalCtx& c,
+                                                     const LineFast& lf,
+                                                     const CoLevel* __restrict__ co,
+                                                     double theta2) {
+  const double lt = log(t);
+  const double l01 = lt - kLn100;
+  const double sqrt_t = sqrt(t);
+  const double inv_t = 1.0 / t;
+  const double inv_sqrt_t = sqrt_t * inv_t;
+  const TPowers w = t_powers_mixed(lt);
   double net = c.gamma_fixed + c.gg_coeff * sqrt_t * (c.t_dust - t);
   {  // [CII] 158
     const double b = exp64(-lf.t_ul[0] * inv_t);
@@ -166,7 +226,7 @@ __device__ __noinline__ double net_heating_fast64(double t, const ThermalCtx& c,
                                                   const LineFast& lf,
                                                   const CoLevel* __restrict__ co,
                                                   double theta2) {
-  return net_heating_fast64_body<true>(t, c, lf, co, theta2);
+  return net_heating_mixed64_body(t, c, lf, co, theta2);
 }
 
 // ------------------------------------------- warp-cooperative FP64 net heating

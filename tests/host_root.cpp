@@ -136,7 +136,7 @@ extern "C" void hr_root_mixed_coop(long n, const double* ctx, const double* t_wa
 extern "C" void hr_net64_mixed(long n, const double* ctx, const double* t, double* out) {
   for (long i = 0; i < n; ++i) {
     ThermalCtx c = make_ctx(ctx + 10 * i);
-    out[i] = net_heating_fast64_body<true>(t[i], c, g_lf, g_co, g_theta2);
+    out[i] = net_heating_mixed64_body(t[i], c, g_lf, g_co, g_theta2);
   }
 }
 

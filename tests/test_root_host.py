@@ -166,7 +166,7 @@ def test_cooperative_net_heating_and_root(lib, contexts):
     """The thermal kernel's warp-cooperative FP64 net heating
     (net_heating_coop64: the 5 fine-structure lines and 40 CO levels as one
     table of two-level lines, coop_line) and the mixed root's lane-wise form
-    (net_heating_fast64_body<true>: power laws as products of T^0.01)
+    (net_heating_mixed64_body: power laws as products of T^0.01)
     against the plain form (net_heating_fast64_body) on the oracle's contexts at 12 temperatures
     over 10 K - 1e5 K: equal to 1e-13 of the heating + cooling scale (the
     table's folded constants and the summation order differ); and the mixed

@@ -487,15 +487,15 @@ def network_bench(args):
 # on `bench.py --profile kernels` / `--profile rt` at 128^3 (2,097,152
 # cells, one kernel per capture, --clock-control none):
 # FP64 flops (DFMA = 2, DADD / DMUL = 1) per cell solve of the mixed
-# chemistry (1,093) and thermal (1,180) kernels on the 14th outer iteration,
+# chemistry (1,093) and thermal (1,043) kernels on the 14th outer iteration,
 # every cell solved with exact roots, and their FP32 flops (723 + 5,978);
-# DRAM bytes of the two launches (read + write: 328.5 + 212.6 and 528.3 +
-# 265.9 MB): the state is streamed once per solve, so the traffic scales
+# DRAM bytes of the two launches (read + write: 328.5 + 212.6 and 536.3 +
+# 301.1 MB): the state is streamed once per solve, so the traffic scales
 # with the cells solved.
-FP64_OPS_PER_CELL_SOLVE = 1092.9 + 1179.9
+FP64_OPS_PER_CELL_SOLVE = 1092.9 + 1042.6
 FP32_OPS_PER_CELL_SOLVE = 723.0 + 5977.7
-DRAM_BYTES_PER_CELL_SOLVE = (328.5 + 212.6 + 528.3 + 265.9) * 1e6 / 2097152
-FP64_PIPE_ACTIVE_NCU = ("85% (chemistry), 70% (thermal): the pipe also runs FP64 compares, "
+DRAM_BYTES_PER_CELL_SOLVE = (328.5 + 212.6 + 536.3 + 301.1) * 1e6 / 2097152
+FP64_PIPE_ACTIVE_NCU = ("85% (chemistry), 72% (thermal): the pipe also runs FP64 compares, "
                         "min/max and FP32<->FP64 conversions; the thermal kernel's remaining "
                         "time is latency of divergent root paths")
 # columns launch (a full pass): FP64-pipe bound (82% busy), 29 FP64 flops

@@ -100,6 +100,8 @@ static void launch_columns(SteadySolver* s, const SteadyParams& par, cudaStream_
   if (s->star) {  // columns towards the star (the cell's own half layer included)
     launch_point_source(s->nx, s->ny, s->nz, s->dens, d.x_h2, d.x_co, s->star_pos, s->star_lum,
                         s->cell, 1, nullptr, nullptr, nullptr, d.u_h2, d.u_co, s->st->sms, str);
+    ss_col_moved_kernel<<<grid_for(s->n, s->st->sms, 8), kThreads, 0, str>>>(
+        s->n, d.u_h2, d.u_co, ColQuiet{d.u_h2_last, d.u_co_last, d.q_moved, par.quiet_in_tol});
     return;
   }
   const ColumnsGrid g = columns_grid(s->nx, s->ny, s->nz);
@@ -136,10 +138,10 @@ static int launch_iteration(SteadySolver* s, bool mixed, const SteadyParams& par
 }
 
 // kernels of one mixed iteration with the ray-set columns (the plain path
-// launches two fewer; the point-source columns take three launches, not one)
+// launches two fewer; the point-source columns take four launches, not one)
 constexpr int kLaunchesPerIteration = 8;
 static int launches_per_iteration(const SteadySolver* s, bool mixed) {
-  return kLaunchesPerIteration - (mixed ? 0 : 2) + (s->star ? 2 : 0);
+  return kLaunchesPerIteration - (mixed ? 0 : 2) + (s->star ? 3 : 0);
 }
 
 }  // namespace p3d

@@ -280,6 +280,18 @@ __global__ void ss_col_mark_kernel(int64_t nx, int64_t ny, int64_t nz,
   }
 }
 
+// Star mode: the point-source columns come from their own kernels, so the
+// worklist's column test (as col_store makes it) is made here for every cell.
+__global__ void ss_col_moved_kernel(int64_t n, const double* __restrict__ u_h2,
+                                    const double* __restrict__ u_co, ColQuiet q) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double uh2 = u_h2[i], uco = u_co[i];
+    q.moved[i] = !(fabs(uh2 - q.h2_last[i]) <= q.tol * fabs(uh2) &&
+                   fabs(uco - q.co_last[i]) <= q.tol * fabs(uco));
+  }
+}
+
 // force: every tile (else those marked in `dirty`, or all when g->cols_all);
 // a tile's mark is cleared when it is recomputed.  A tile left out keeps its
 // columns from the last pass, computed from the same layers.

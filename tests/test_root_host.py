@@ -200,14 +200,16 @@ def test_cooperative_net_heating_and_root(lib, contexts):
     assert np.mean(rel <= 1e-9) >= 0.999, np.sort(rel)[-5:]
 
 
-def test_mixed_root_in_the_outer_loop_reaches_the_plain_fixed_point(lib, monkeypatch):
+@pytest.mark.parametrize("coop", [False, True])
+def test_mixed_root_in_the_outer_loop_reaches_the_plain_fixed_point(lib, monkeypatch, coop):
     """The oracle's steady method on the 24^3 slab cut, once with its plain
     FP64 roots and once with the host-built mixed root in their place (warm
     starts, replayed decisions and the one-evaluation pinned roots across
-    outer iterations, tol 1e-10): same iteration count, and every cell's T
-    and abundances within 1e-6 of the plain fixed point.  (The root before
-    its Newton slope was confined to T's continuous piece left 20 cells of
-    this grid 1e-6 to 9e-3 away.)"""
+    outer iterations, tol 1e-10; coop: every FP64 evaluation in the
+    cooperative form the thermal kernel uses for short worklists): same
+    iteration count, and every cell's T and abundances within 1e-6 of the
+    plain fixed point.  (The root before its Newton slope was confined to
+    T's continuous piece left 20 cells of this grid 1e-6 to 9e-3 away.)"""
     from prism3d_gb300 import fields
     from prism3d_gb300.core import directional_G0
     dens = fields.orion_bar_slab(24, seed=1)
@@ -231,7 +233,15 @@ def test_mixed_root_in_the_outer_loop_reaches_the_plain_fixed_point(lib, monkeyp
                          margin=np.zeros(n, np.float32), ctx=None)
         delta = (np.full(n, np.inf) if state["ctx"] is None else
                  np.max(np.abs(c - state["ctx"]) / np.maximum(np.abs(c), 1e-300), axis=1))
-        t, ev, st = _mixed(lib, c, state["t"], delta, state["node"], state["margin"])
+        if coop:
+            t = np.zeros(n)
+            ev = np.zeros(n, np.int32)
+            st = np.zeros(n, np.int32)
+            lib.hr_root_mixed_coop(ctypes.c_long(n), _p(c), _p(state["t"]), _p(delta),
+                                   _p(state["node"]), _p(state["margin"]), ctypes.c_double(TOL),
+                                   _p(t), _p(ev), _p(st))
+        else:
+            t, ev, st = _mixed(lib, c, state["t"], delta, state["node"], state["margin"])
         state["t"], state["ctx"] = t, c
         return t, ev.astype(np.int64), st
 

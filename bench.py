@@ -275,7 +275,8 @@ def run_gb300(args, ws, rank, local):
                      "counts_source": "ncu instruction and DRAM counters of this pass's "
                                       "chemistry and thermal launches (bench.py --profile "
                                       "kernels, 128^3)",
-                     "fp64_pipe_active_ncu": FP64_PIPE_ACTIVE_NCU},
+                     "fp64_pipe_active_ncu": FP64_PIPE_ACTIVE_NCU,
+                     "counts_at_commit": COUNTS_AT_COMMIT["cell"]},
         "roofline_hbm": {"kernel": "ss_columns_kernel (3 axes x 2 directions, one launch per "
                                    "outer iteration)",
                          "bound": "hbm", "achieved": col_gbs, "peak": hbm, "unit": "GB/s",
@@ -286,7 +287,8 @@ def run_gb300(args, ws, rank, local):
                                  "layers are partly L2-resident, the columns stay in L2 "
                                  "(ncu, bench.py --profile kernels); a full pass, where a "
                                  "mixed run's last iterations recompute only the tiles "
-                                 "holding rewritten cells"},
+                                 "holding rewritten cells",
+                         "counts_at_commit": COUNTS_AT_COMMIT["columns"]},
         "kernel_times_ms": kt,
         "fp64_net_heating_evals_per_cell_iter": float(np.mean(hist[:, 6]) / n),
         "gpu_launches": int(sum(launches)),
@@ -425,7 +427,8 @@ def rt_dropin_bench(dens, g0, cell, nside, state, hbm, peak_kind, fp64_peak, wor
                            "kernel on this GPU", "traffic": RT_DRAM_BYTES_PER_CELL[workload] * n,
                            "per_unit": f"{RT_FP64_OPS_PER_CELL[workload]:.0f} FP64 flops per cell "
                                        "(walk + merge, 48 rays; ncu counts, "
-                                       "bench.py --profile rt)"}
+                                       "bench.py --profile rt)",
+                           "counts_at_commit": COUNTS_AT_COMMIT["rt"]}
     return res
 
 
@@ -506,6 +509,10 @@ COLUMNS_DRAM_BYTES_PER_CELL = (82.1 + 13.5) * 1e6 / 2097152
 # and DRAM bytes per cell of the two launches
 RT_FP64_OPS_PER_CELL = {"slab128": 684.0 + 12.0}
 RT_DRAM_BYTES_PER_CELL = {"slab128": (233.6 + 460.8 + 344.5 + 74.4) * 1e6 / 2097152}
+# the source revision each capture above ran on (none of the captured
+# kernels has changed since)
+COUNTS_AT_COMMIT = {"cell": {"ss_chem_kernel": "4093bfe", "ss_thermal_kernel": "95ae15a"},
+                    "columns": "e85e9b0", "rt": "e85e9b0"}
 STATE_KEYS = ("T_gas", "x_HI", "x_H2", "x_Cp", "x_C", "x_CO", "x_O", "x_e")
 
 

@@ -50,8 +50,10 @@ struct SteadySolver {
   SteadyParams graph_par;
   int64_t iters_done = 0;
   // launch shape of the per-cell chemistry / thermal kernels (threads per
-  // block, blocks per SM of the grid-stride loop); p3d_steady_autotune sets it
-  int cell_threads = kThreads, cell_per_sm = 4;
+  // block, blocks per SM of the grid-stride loop); p3d_steady_autotune sets
+  // it.  Default: the shape it picks on GB300 for the 128^3 slab (more
+  // blocks than fit an SM: the work queue hands cells to the blocks resident)
+  int cell_threads = 128, cell_per_sm = 16;
   int64_t launches = 0;  // kernels launched since the last reset
   cudaEvent_t ev_start = nullptr, ev_stop = nullptr;  // reset .. end of last run
   double last_dmax = INFINITY;

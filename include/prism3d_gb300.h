@@ -240,7 +240,8 @@ int p3d_fuv_field_3d_dev(int64_t nx, int64_t ny, int64_t nz, const double *densi
  * above.
  *
  * p3d_steady_create  copy density, ray set, PE table and line data to the
- *                    device (host pointers); x_c_total / x_o_total are the
+ *                    device (host pointers); at most 2^31 - 1 cells
+ *                    (P3D_EINVAL above); x_c_total / x_o_total are the
  *                    gas-phase C and O abundances, t_init the initial T_gas,
  *                    h2_sigmas the THEMIS H2-formation area sums (nano,
  *                    large carbon, silicate; themis_tables.py:255-276).

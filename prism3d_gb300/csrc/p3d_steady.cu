@@ -167,10 +167,14 @@ int p3d_steady_create(p3d_steady_t** out, int64_t nx, int64_t ny, int64_t nz,
                       const double* oi63, const double* oi145, const double* ci) {
   if (!out) return set_error(P3D_EINVAL, "null handle pointer");
   *out = nullptr;
+  if (nx <= 0 || ny <= 0 || nz <= 0) return set_error(P3D_EINVAL, "grid must be non-empty");
+  // the worklist holds 32-bit cell indices
+  if (nx > INT32_MAX / ny || nx * ny > INT32_MAX / nz)
+    return set_error(P3D_EINVAL, "grid of %lld x %lld x %lld cells exceeds 2^31 - 1 cells",
+                     (long long)nx, (long long)ny, (long long)nz);
   DeviceState* st;
   int rc = get_state(&st);
   if (rc) return rc;
-  if (nx <= 0 || ny <= 0 || nz <= 0) return set_error(P3D_EINVAL, "grid must be non-empty");
   if (!density || !g0_ext || !dirs || !weights || !pe_table || !bin_sigma_abs ||
       !bin_dn_da_da || !bin_is_nano || !h2_sigmas || !cii || !oi63 || !oi145 || !ci)
     return set_error(P3D_EINVAL, "null argument");

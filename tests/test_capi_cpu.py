@@ -108,3 +108,19 @@ def test_no_gpu_raises(lib):
     with pytest.raises(lib.P3DError) as ei:
         core.total_heating_cooling(*ctx, *line_params(), np.ones(n), np.ones(n), np.ones(n))
     assert ei.value.code == -2
+
+
+def test_steady_create_rejects_oversized_grid(lib):
+    """The steady driver's worklist holds 32-bit cell indices: a grid of more
+    than 2^31 - 1 cells is refused as a bad argument, before any device work
+    (so with or without a GPU), and no handle is returned."""
+    import ctypes
+    h = ctypes.c_void_p(1)
+    one = np.ones(64)
+    p = lib.dptr
+    args = [1 << 11, 1 << 11, 1 << 10, p(one), p(one), 1, 1.0, p(one), p(one), 1, 2e-16,
+            1e-4, 3e-4, 100.0, p(one), 1, -1.0, 0.1, 2, 0.01, 0.1, 2, p(one), p(one), p(one),
+            p(one), p(one), p(one), p(one), p(one)]
+    rc = lib.lib.p3d_steady_create(ctypes.byref(h), *args)
+    assert rc == -1 and not h.value
+    assert b"2^31" in lib.lib.p3d_last_error()

@@ -124,3 +124,29 @@ def test_steady_create_rejects_oversized_grid(lib):
     rc = lib.lib.p3d_steady_create(ctypes.byref(h), *args)
     assert rc == -1 and not h.value
     assert b"2^31" in lib.lib.p3d_last_error()
+
+
+def test_null_handles_refused(lib):
+    """Every steady-driver and network entry point that takes a handle
+    refuses a null one with P3D_EINVAL (no dereference, no device work);
+    destroying a null handle is a no-op."""
+    import ctypes
+    refused = []
+    for name, argtypes in lib.SIGNATURES.items():
+        if not name.startswith(("p3d_steady_", "p3d_network_")) or name.endswith("_create"):
+            continue
+        args = []
+        for t in argtypes:
+            if t in (ctypes.c_double, ctypes.c_float):
+                args.append(0.0)
+            elif t in (ctypes.c_int, ctypes.c_int32, ctypes.c_int64, ctypes.c_uint32):
+                args.append(0)
+            else:
+                args.append(None)
+        rc = getattr(lib.lib, name)(*args)
+        if name.endswith("_destroy"):
+            assert rc == 0, name
+        else:
+            assert rc == -1, (name, rc)
+            refused.append(name)
+    assert len(refused) >= 24, refused

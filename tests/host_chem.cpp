@@ -42,7 +42,11 @@ extern "C" void hc_chem_steady(long n, const double* n_h, const double* kpd0,
     cc.u_co = u_co[i];
     cc.ds = 0.0;
     cc.b_dop = b_dop;
-    chem_prepare(cc);
+    // the mixed kernel prepares the shielding in its own forms (FAST)
+    if (mixed)
+      chem_prepare<true>(cc);
+    else
+      chem_prepare<false>(cc);
     double* yi = y + 5 * i;
     for (int c = 0; c < 5; ++c) yi[c] = fmax(yi[c], 1e-30);
     int it = 0;

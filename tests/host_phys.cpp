@@ -17,18 +17,17 @@
 
 using namespace p3d;
 
-extern "C" void hp_fsh_h2(long n, const double* nh2, double b, double* out) {
-  for (long i = 0; i < n; ++i) {
-    double d;
-    out[i] = fsh_h2(nh2[i], b, &d);
-  }
+// fast != 0: the mixed path's forms (template argument FAST)
+extern "C" void hp_fsh_h2(long n, const double* nh2, double b, double* out, double* dfdn,
+                          int fast) {
+  for (long i = 0; i < n; ++i)
+    out[i] = fast ? fsh_h2<true>(nh2[i], b, dfdn + i) : fsh_h2<false>(nh2[i], b, dfdn + i);
 }
 
-extern "C" void hp_fsh_co(long n, const double* nco, const double* nh2, double* out) {
-  for (long i = 0; i < n; ++i) {
-    double d;
-    out[i] = fsh_co(nco[i], nh2[i], &d);
-  }
+extern "C" void hp_fsh_co(long n, const double* nco, const double* nh2, double* out,
+                          double* d_h2, int fast) {
+  for (long i = 0; i < n; ++i)
+    out[i] = fast ? fsh_co<true>(nco[i], nh2[i], d_h2 + i) : fsh_co<false>(nco[i], nh2[i], d_h2 + i);
 }
 
 extern "C" void hp_cr_rate(long n, const double* nh, double zeta0, double* out) {
@@ -41,8 +40,10 @@ extern "C" void hp_tdust(long n, const double* g0, const double* av, const doubl
 }
 
 extern "C" void hp_h2_form(long n, const double* tg, const double* td, const double* fnano,
-                           double s_nano, double s_lc, double s_sil, double* out) {
-  for (long i = 0; i < n; ++i) out[i] = h2_form(tg[i], td[i], fnano[i], s_nano, s_lc, s_sil);
+                           double s_nano, double s_lc, double s_sil, double* out, int fast) {
+  for (long i = 0; i < n; ++i)
+    out[i] = fast ? h2_form<true>(tg[i], td[i], fnano[i], s_nano, s_lc, s_sil)
+                  : h2_form<false>(tg[i], td[i], fnano[i], s_nano, s_lc, s_sil);
 }
 
 // PE heating per cell from the condensed tables a_nano, a_rest (n_psi x

@@ -5,7 +5,9 @@ self-shielding at five grid-mean temperatures, CO shielding, cosmic-ray
 attenuation for two zeta_0, dust temperature, the H2 formation rate and
 the PE heating (condensed tables formed here as pe_condense_kernel does) on
 4000 points including the branch edges.  Tolerance 1e-13 relative (FP64
-pow/exp/log10 of the host library against NumPy's)."""
+pow/exp/log10 of the host library against NumPy's); the mixed path's forms
+of the shielding factors and the H2 formation rate to the same values
+within the tolerances in FAST_TOL."""
 import ctypes
 
 import numpy as np
@@ -25,16 +27,37 @@ def _c(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
-def test_shielding_and_cosmic_rays(lib, golden):
+# the mixed path's forms of the shielding factors and the H2 formation
+# rate (FAST: one denominator, logarithms and exp64 instead of divisions,
+# pow() and exp()) against the same reference values (measured: fsh_h2
+# 6e-16, fsh_co 4e-14, h2_form 6e-16); their N_H2 derivatives against the plain forms', to
+# 1e-13 of the largest (the CO one is a difference of two terms)
+FAST_TOL = {"fsh_h2": 1e-13, "fsh_co": 1e-13, "h2_form": 1e-13}
+
+
+@pytest.mark.parametrize("fast", [0, 1])
+def test_shielding_and_cosmic_rays(lib, golden, fast):
     g = golden("elementwise")
     n = g["N_H2"].size
     out = np.zeros(n)
+    d = np.zeros(n)
+    d_plain = np.zeros(n)
     for i, tm in enumerate(g["T_mean"]):
         b = np.sqrt(2.0 * O.k_boltz * tm / O.m_H2) / 1e5
-        lib.hp_fsh_h2(ctypes.c_long(n), _p(_c(g["N_H2"])), ctypes.c_double(b), _p(out))
-        np.testing.assert_allclose(out, g[f"fsh_h2_{i}"], rtol=1e-13, atol=0)
-    lib.hp_fsh_co(ctypes.c_long(n), _p(_c(g["N_CO"])), _p(_c(g["N_H2"])), _p(out))
-    np.testing.assert_allclose(out, g["fsh_co"], rtol=1e-13, atol=0)
+        lib.hp_fsh_h2(ctypes.c_long(n), _p(_c(g["N_H2"])), ctypes.c_double(b), _p(out), _p(d),
+                      ctypes.c_int(fast))
+        np.testing.assert_allclose(out, g[f"fsh_h2_{i}"],
+                                   rtol=FAST_TOL["fsh_h2"] if fast else 1e-13, atol=0)
+        lib.hp_fsh_h2(ctypes.c_long(n), _p(_c(g["N_H2"])), ctypes.c_double(b), _p(out),
+                      _p(d_plain), ctypes.c_int(0))
+        np.testing.assert_allclose(d, d_plain, rtol=1e-13, atol=1e-13 * np.abs(d_plain).max())
+    lib.hp_fsh_co(ctypes.c_long(n), _p(_c(g["N_CO"])), _p(_c(g["N_H2"])), _p(out), _p(d),
+                  ctypes.c_int(fast))
+    np.testing.assert_allclose(out, g["fsh_co"], rtol=FAST_TOL["fsh_co"] if fast else 1e-13,
+                               atol=0)
+    lib.hp_fsh_co(ctypes.c_long(n), _p(_c(g["N_CO"])), _p(_c(g["N_H2"])), _p(out), _p(d_plain),
+                  ctypes.c_int(0))
+    np.testing.assert_allclose(d, d_plain, rtol=1e-13, atol=1e-13 * np.abs(d_plain).max())
     n = g["N_H"].size
     out = np.zeros(n)
     for z0 in (2e-16, 5e-16):
@@ -42,7 +65,8 @@ def test_shielding_and_cosmic_rays(lib, golden):
         np.testing.assert_allclose(out, g[f"zeta_{z0:g}"], rtol=1e-13, atol=0)
 
 
-def test_dust_temperature_and_h2_formation(lib, golden):
+@pytest.mark.parametrize("fast", [0, 1])
+def test_dust_temperature_and_h2_formation(lib, golden, fast):
     from prism3d_gb300.tables import DustTables
     g = golden("elementwise")
     tb = DustTables()
@@ -54,8 +78,9 @@ def test_dust_temperature_and_h2_formation(lib, golden):
     rh2 = np.zeros(n)
     lib.hp_h2_form(ctypes.c_long(n), _p(_c(g["Tg"])), _p(td), _p(_c(g["fn"])),
                    ctypes.c_double(tb.sigma_nano), ctypes.c_double(tb.sigma_largeC),
-                   ctypes.c_double(tb.sigma_Sil), _p(rh2))
-    np.testing.assert_allclose(rh2, g["RH2"], rtol=1e-13, atol=0)
+                   ctypes.c_double(tb.sigma_Sil), _p(rh2), ctypes.c_int(fast))
+    np.testing.assert_allclose(rh2, g["RH2"], rtol=FAST_TOL["h2_form"] if fast else 1e-13,
+                               atol=0)
 
 
 def test_pe_heating(lib, golden):
